@@ -1,0 +1,139 @@
+/*
+ * sigma_gb300 — GB300-native (sm_103a) SIGmA inprocessing round of ParaFROST.
+ *
+ * C ABI of libsigma_gb300.so: plain pointers and sizes, no C++ or torch types.
+ * One context holds one formula resident in device memory (clause store,
+ * occurrence table, per-variable state) and runs sigmify rounds on it.
+ *
+ * Literal encoding is the reference solver's: lit = 2*var + sign, variables
+ * 1..num_vars, sign 1 = negative (src/cpu/const.h:73-78). Literal slots 0 and 1
+ * are unused.
+ *
+ * Every entry point returns a pf_status; none exits the process or resets the
+ * device. Errors are sticky per context until pf_sigma_destroy.
+ */
+#ifndef SIGMA_GB300_H
+#define SIGMA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. Replaces the reference's simpstate codes and exit paths
+ * (src/gpu/const.cuh:29-32, definitions.cuh:51-74). */
+typedef enum {
+    PF_OK = 0,
+    PF_UNSAT = 1,     /* the round proved the formula unsatisfiable (learnEmpty) */
+    PF_EINVAL = -1,   /* bad argument (literal out of range, null pointer, ...) */
+    PF_ENOMEM = -2,   /* device memory budget exceeded (CNFALLOC_FAIL/OTALLOC_FAIL) */
+    PF_ETIMEOUT = -3, /* a bounded device wait gave up */
+    PF_EDEVICE = -4,  /* CUDA error; pf_last_error() has the text */
+    PF_ESTATE = -5,   /* call out of order (e.g. round before upload) */
+} pf_status;
+
+/* Simplifier options: the reference's option names and defaults
+ * (src/cpu/options.cpp:24-46, derivation rules at options.cpp:281-311).
+ * Fill with pf_default_options() and pass to pf_sigma_create. */
+typedef struct {
+    int32_t phases;          /* "phases"       = 5     */
+    int32_t all;             /* "all"          = 0  (=> ve, ve+, bce, ere) */
+    int32_t ve;              /* "ve"           = 1     */
+    int32_t ve_plus;         /* "ve+"          = 1     */
+    int32_t sub;             /* "sub"          = 1     */
+    int32_t bce;             /* "bce"          = 0     */
+    int32_t ere;             /* "ere"          = 1     */
+    int32_t ve_lbound;       /* "velbound"     = 0     */
+    int32_t ve_clause_max;   /* "veclausemax"  = 100 (0: no limit) */
+    int32_t ve_phase_min;    /* "vephasemin"   = 500   */
+    int32_t mu_pos;          /* "mupos"        = 32    */
+    int32_t mu_neg;          /* "muneg"        = 32    */
+    int32_t xor_max_arity;   /* "xormaxarity"  = 10    */
+    int32_t sub_max;         /* "submax"       = 3000  */
+    int32_t bce_max;         /* "bcemax"       = 3000  */
+    int32_t ere_max;         /* "eremax"       = 3000  */
+    int32_t ere_clause_max;  /* "ereclausemax" = 1000 (0: no limit) */
+    int32_t lcve_min;        /* "lcvemin"      = 1     */
+    int32_t gc_freq;         /* "gcfreq"       = 2 (0: never compact inside the round) */
+    /* GB300 extras (no counterpart in the reference) */
+    int32_t dump_level;      /* 0: off, 1: per-phase summaries, 2: every stage */
+    int32_t reserved[7];
+} pf_options;
+
+/* Per-round statistics (the reference's stage report, src/cpu/statistics.cpp:28-41,
+ * plus the device-side measurements). Times are device milliseconds. */
+typedef struct {
+    int32_t status;           /* pf_status of the round */
+    int32_t phases_run;
+    uint64_t clauses_before, literals_before;
+    uint64_t clauses_after, literals_after;
+    uint64_t eliminated_vars; /* variables eliminated by this round */
+    uint64_t units;           /* assigned literals on the trail after the round */
+    uint64_t resolved_words;  /* witness-stack length */
+    double ms_total;          /* device time of the round */
+    double ms_stage[12];      /* ot, prop, lcve, sort, sub, ve, bce, ere, gc, count, upload, download */
+    uint64_t algorithmic_bytes; /* bytes the round's kernels must move (HBM roofline numerator) */
+    uint32_t kernel_launches;   /* kernels launched by the round */
+    uint32_t reserved[3];
+} pf_round_stats;
+
+typedef struct pf_sigma_ctx pf_sigma_ctx;
+
+/* Fills *o with the reference defaults. */
+void pf_default_options(pf_options* o);
+
+/* Applies the reference's option derivation (options.cpp:304-311) in place. */
+void pf_derive_options(pf_options* o);
+
+/* Creates a context on the current CUDA device. Replaces ParaFROST::optSimp()
+ * + cuMM pool set-up (src/gpu/simplify.cu:254-270, memory.cu). *out is NULL on error. */
+pf_status pf_sigma_create(const pf_options* opts, pf_sigma_ctx** out);
+
+/* Uploads a formula: clause c has literals lits[offsets[c] .. offsets[c+1]).
+ * learnt may be NULL (all original). Literal order inside a clause is free; the
+ * upload sorts literals and computes signatures, as extract() does
+ * (src/cpu/simplify.cpp:95-113, src/gpu/transfer.cu:24-42 + kernels.cu:61-70).
+ * Host buffers; copies are issued on the context stream. */
+pf_status pf_sigma_upload(pf_sigma_ctx* ctx, uint32_t num_vars,
+                          const uint32_t* lits, const uint64_t* offsets, uint64_t num_clauses,
+                          const uint8_t* learnt);
+
+/* Same as pf_sigma_upload, with lits/offsets/learnt already in device memory. */
+pf_status pf_sigma_upload_device(pf_sigma_ctx* ctx, uint32_t num_vars,
+                                 const uint32_t* d_lits, const uint64_t* d_offsets, uint64_t num_clauses,
+                                 const uint8_t* d_learnt);
+
+/* Runs one sigmify round (ParaFROST::sigmifying(), src/cpu/simplify.cpp:157-232,
+ * GPU twin src/gpu/simplify.cu:155-234) on the resident formula. */
+pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats);
+
+/* Sizes of the simplified formula, for sizing pf_sigma_download buffers. */
+pf_status pf_sigma_result_sizes(pf_sigma_ctx* ctx, uint64_t* num_clauses, uint64_t* num_literals,
+                                uint64_t* num_units, uint64_t* num_resolved);
+
+/* Copies the simplified formula back to host buffers (any pointer may be NULL):
+ * surviving clauses in clause-store order (lits/offsets/learnt), the trail of
+ * assigned literals, the witness stack (the reference's model.resolved words,
+ * src/cpu/model.cpp:334-379) and one eliminated flag per variable (index 0 unused).
+ * Replaces cacheCNF/cacheUnits/cacheResolved/markEliminated (src/gpu/transfer.cu:68-165). */
+pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets, uint8_t* learnt,
+                            uint32_t* units, uint32_t* resolved, uint8_t* eliminated);
+
+/* Writes the per-stage round dump of the last round to path (dump_level > 0). */
+pf_status pf_sigma_write_dump(pf_sigma_ctx* ctx, const char* path);
+
+/* Device bytes held by the context. */
+pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes);
+
+void pf_sigma_destroy(pf_sigma_ctx* ctx);
+
+/* Text of the last error on this thread. */
+const char* pf_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIGMA_GB300_H */

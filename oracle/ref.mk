@@ -1,0 +1,28 @@
+# Builds the reference ParaFROST CPU solver (the SIGmA simplifier lives in it)
+# straight from its sources under REFDIR with g++, without the reference's own
+# installer. Outputs go only to oracle/_ref/. Test infrastructure, never shipped.
+#
+#   make -f oracle/ref.mk REFDIR=/path/to/ParaFROST -j8
+REFDIR ?= /root/reference
+OUT    := oracle/_ref
+SRCDIR := $(REFDIR)/src/cpu
+CXX    ?= g++
+# Same optimisation flags as the reference installer's release mode, plus the two
+# -include flags that g++ 13 needs because the sources rely on transitive includes.
+CXXFLAGS := -std=c++17 -DNDEBUG -O3 -fPIC -w -include cstdint -include cstddef -Ioracle
+SRCS := $(filter-out $(SRCDIR)/main.cpp,$(sort $(wildcard $(SRCDIR)/*.cpp)))
+OBJS := $(patsubst $(SRCDIR)/%.cpp,$(OUT)/obj/%.o,$(SRCS))
+
+all: $(OUT)/libpfref.a $(OUT)/sigma_ref
+
+$(OUT)/obj/%.o: $(SRCDIR)/%.cpp
+	@mkdir -p $(OUT)/obj
+	$(CXX) $(CXXFLAGS) -I$(SRCDIR) -c $< -o $@
+
+$(OUT)/libpfref.a: $(OBJS)
+	ar rcs $@ $^
+
+$(OUT)/sigma_ref: oracle/ref_harness.cpp $(OUT)/libpfref.a
+	$(CXX) $(CXXFLAGS) -I$(SRCDIR) $< -o $@ $(OUT)/libpfref.a
+
+.PHONY: all

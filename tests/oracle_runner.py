@@ -1,0 +1,72 @@
+"""Test-side access to the oracles (test infrastructure only).
+
+* ``run_oracle``: the CPU restatement in oracle/sigma_oracle.cpp, loaded with ctypes
+  from oracle/_build/libsigma_oracle.so (built by ``__graft_entry__.build()``).
+* ``run_reference``: the compiled reference harness oracle/_ref/sigma_ref (built from
+  the reference sources by oracle/ref.mk; only present where the reference is).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+from parafrost_gb300 import cnfgen, rounddump
+from parafrost_gb300.options import Options
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "libsigma_oracle.so")
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", "sigma_ref")
+
+_lib = None
+
+
+def oracle_lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            raise RuntimeError(f"oracle library missing: {ORACLE_SO} (run __graft_entry__.build())")
+        _lib = ctypes.CDLL(ORACLE_SO)
+        _lib.oracle_sigmify.restype = ctypes.c_int
+        _lib.oracle_sigmify.argtypes = [
+            ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+            ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    return _lib
+
+
+def run_oracle(num_vars, lits, offsets, opts: Options | None = None, level: int = 2, learnt=None):
+    """Run the restated round; returns (status, records, seconds)."""
+    opts = opts or Options(all=1)
+    o = opts.derived().to_struct()
+    lits = np.ascontiguousarray(lits, dtype=np.uint32)
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+    lp = None
+    if learnt is not None:
+        learnt = np.ascontiguousarray(learnt, dtype=np.uint8)
+        lp = learnt.ctypes.data
+    secs = ctypes.c_double(0.0)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "oracle.dump")
+        st = oracle_lib().oracle_sigmify(ctypes.addressof(o), num_vars, lits.ctypes.data, offsets.ctypes.data,
+                                         offsets.size - 1, lp, path.encode(), level, ctypes.byref(secs))
+        recs = rounddump.read(path)
+    return st, recs, secs.value
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_BIN)
+
+
+def run_reference(num_vars, lits, offsets, opts: Options | None = None, level: int = 2):
+    """Run the compiled reference round through its own DIMACS parser; returns records."""
+    opts = opts or Options(all=1)
+    with tempfile.TemporaryDirectory() as td:
+        cnf = os.path.join(td, "f.cnf")
+        dump = os.path.join(td, "ref.dump")
+        cnfgen.to_dimacs(cnf, num_vars, lits, offsets)
+        args = [REF_BIN, cnf, dump, str(level)] + opts.reference_flags()
+        subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        return rounddump.read(dump)
