@@ -1,0 +1,275 @@
+"""Benchmark: one sigmify round (ParaFROST's GPU inprocessing round) per step.
+
+Workload (default): Tseitin encoding of a seeded random AIG with 2M AND and
+200k XOR gates over 50k inputs (6.8M clauses, 16.4M literals, 2.25M variables),
+synthetic, generated in-process. A step = device-side awaken (copy of the
+resident input + literal sort + signatures) + one full round with the
+reference's default phase settings and -all (VE, SUB, BCE, ERE). Metric unit:
+input clauses simplified per second (whole job; N GPUs run N independent
+replicas: the round does not shard, so there is no collective).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+The reference arm times the reference's CPU simplifier on the host cores: the
+compiled reference (oracle/_ref) when present, else the oracle port of it
+(oracle/_build), on a bounded sample of the same workload (a 1/8-size AIG of the
+same generator), in the same unit.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+WORKLOADS = {
+    "aig-2.2m": dict(gen="aig_tseitin", kw=dict(num_inputs=50_000, num_and=2_000_000, num_xor=200_000, seed=1),
+                     sample_kw=dict(num_inputs=6_250, num_and=250_000, num_xor=25_000, seed=1)),
+    "community-20m": dict(gen="community", kw=dict(seed=1),
+                          sample_kw=dict(num_vars=2_000_000, num_clauses=8_000_000, seed=1)),
+    "ksat3-10k": dict(gen="random_ksat", kw=dict(num_vars=10_000, num_clauses=42_600, k=3, seed=1),
+                      sample_kw=dict(num_vars=10_000, num_clauses=42_600, k=3, seed=1)),
+}
+METRIC = "sigmify round ms & HBM GB/s; batched CNFs/s, p50/p99 latency vs plain GPU"
+UNIT = "clauses/s"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def make_workload(name: str, sample: bool = False):
+    from parafrost_gb300 import cnfgen
+    spec = WORKLOADS[name]
+    kw = spec["sample_kw"] if sample else spec["kw"]
+    return getattr(cnfgen, spec["gen"])(**kw)
+
+
+def cpu_round_seconds(nv, lits, off) -> tuple:
+    """Reference CPU simplifier on one formula: (seconds, kind)."""
+    import oracle_runner as orr
+    from parafrost_gb300.options import Options
+    if orr.reference_available():
+        recs = orr.run_reference(nv, lits, off, Options(all=1), level=0)
+        t = [d for (k, ph, st, d) in recs if k == "timing"][0]
+        return (int(t[0]) | (int(t[1]) << 32)) / 1e6, "reference"
+    from parafrost_gb300 import build
+    build.build_oracle()
+    st, _, secs = orr.run_oracle(nv, lits, off, Options(all=1), level=0)
+    return secs, "port"
+
+
+def run_reference(args) -> dict:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return None
+    nv, lits, off = make_workload(args.workload, sample=True)
+    ncls = off.size - 1
+    for _ in range(args.warmup):
+        cpu_round_seconds(nv, lits, off)
+    times = []
+    kind = "port"
+    for _ in range(args.steps):
+        s, kind = cpu_round_seconds(nv, lits, off)
+        times.append(s)
+    tot = float(np.sum(times))
+    value = ncls * args.steps / tot
+    sample = f"{WORKLOADS[args.workload]['sample_kw']} ({ncls} clauses), one full round per step, 1 thread"
+    return {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic", "config": {"workload": args.workload, "sample": True},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def flush_l2(buf):
+    buf.add_(1)
+
+
+def run_ours(args) -> dict:
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from parafrost_gb300.options import Options
+    from parafrost_gb300.sigma import Simplifier
+
+    nv, lits, off = make_workload(args.workload)
+    ncls = off.size - 1
+    dev = torch.device("cuda", local)
+    d_lits = torch.from_numpy(lits.view(np.int32)).to(dev)
+    d_off = torch.from_numpy(off.view(np.int64)).to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    opts = Options(all=1)
+    s = Simplifier(opts)
+
+    def step():
+        s.awaken_device(nv, d_lits.data_ptr(), d_off.data_ptr(), ncls)
+        return s.sigmify()
+
+    for _ in range(max(args.warmup, 3)):
+        st = step()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    for i in range(args.steps):
+        flush_l2(flush)
+        ev[i][0].record()
+        st = step()
+        ev[i][1].record()
+        stats.append(st)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_ms = float(np.sum(step_ms))
+    if world > 1:
+        t = torch.tensor([tot_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    ms = tot_ms / args.steps
+    value = world * ncls * args.steps / (tot_ms / 1e3)
+    last = stats[-1]
+    round_ms = float(np.mean([x.ms_total for x in stats]))
+    alg = float(np.mean([x.algorithmic_bytes for x in stats]))
+    launches = int(np.sum([x.kernel_launches for x in stats]))
+    stage_ms = {k: float(np.mean([x.as_dict()["ms_stage"][k] for x in stats])) for k in stats[0].as_dict()["ms_stage"]}
+
+    # e2e through the C ABI with host buffers: upload (H2D), round, download (D2H)
+    pin_l = torch.from_numpy(lits.view(np.int32)).pin_memory()
+    pin_o = torch.from_numpy(off.view(np.int64)).pin_memory()
+    hl, ho = pin_l.numpy().view(np.uint32), pin_o.numpy().view(np.uint64)
+    e2e_steps = max(1, min(args.steps, 5))
+    d2h = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.awaken(nv, hl, ho)
+        s.sigmify()
+        res = s.result()
+        d2h = res.lits.nbytes + res.offsets.nbytes + res.units.nbytes + res.resolved.nbytes + res.eliminated.nbytes
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = world * ncls / e2e_s
+
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg / (round_ms / 1e3) / 1e9
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+           "config": {"workload": args.workload, "clauses": int(ncls), "literals": int(lits.size), "vars": int(nv),
+                      "options": "-all, phases=5", "l2": "flushed between steps (256 MB write)",
+                      "parallelism": f"replicas x{world}"},
+           "round_ms": round_ms, "stage_ms": stage_ms,
+           "result": {"clauses_after": int(last.clauses_after), "phases": int(last.phases_run),
+                      "status": int(last.status)},
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "scope": "whole round: algorithmic bytes / round device time",
+                        "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"},
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(lits.nbytes + off.nbytes),
+                   "d2h_bytes_per_step": int(d2h)},
+           "gpu_launches": launches, "clocks": clk}
+    s.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        snv, sl, so = make_workload(args.workload, sample=True)
+        secs, kind = cpu_round_seconds(snv, sl, so)
+        out["cpu_baseline"] = {"value": (so.size - 1) / secs, "unit": UNIT, "cores": 1, "kind": kind,
+                               "sample": f"{WORKLOADS[args.workload]['sample_kw']} ({so.size - 1} clauses), one round"}
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="aig-2.2m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        out = run_reference(args)
+    else:
+        from parafrost_gb300 import build
+        build.build_cuda()
+        out = run_ours(args)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

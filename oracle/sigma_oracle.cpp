@@ -1169,3 +1169,31 @@ int oracle_sigmify(const pf_options* opts, uint32_t num_vars, const uint32_t* li
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- sort replica check
+// Checks the product's replica of libstdc++'s std::sort (parafrost_gb300/csrc/
+// introsort.cuh, used on the device for occurrence lists longer than 20) against
+// std::sort itself on random keys with many ties: returns the number of trials
+// whose permutation differs.
+#include "../parafrost_gb300/csrc/introsort.cuh"
+#include <random>
+
+extern "C" long oracle_check_introsort(uint64_t seed, int trials) {
+    struct E { uint32_t key, id; };
+    std::mt19937_64 rng(seed);
+    long bad = 0;
+    for (int t = 0; t < trials; t++) {
+        const int n = (t % 7 == 0) ? (int)(rng() % 3000) : (int)(rng() % 200);
+        const uint32_t kmax = 1 + (uint32_t)(rng() % ((t % 3 == 0) ? 3 : 50));
+        std::vector<E> a(n);
+        for (int i = 0; i < n; i++) a[i] = E{(uint32_t)(rng() % kmax), (uint32_t)i};
+        if (t % 11 == 0) std::sort(a.begin(), a.end(), [](E x, E y) { return x.key < y.key; });
+        if (t % 13 == 0) std::reverse(a.begin(), a.end());
+        std::vector<E> b = a;
+        auto cmp = [](const E& x, const E& y) { return x.key < y.key; };
+        std::sort(a.begin(), a.end(), cmp);
+        sigma::std_sort_replica(b.data(), b.data() + n, cmp);
+        for (int i = 0; i < n; i++) if (a[i].id != b[i].id) { bad++; break; }
+    }
+    return bad;
+}

@@ -1,0 +1,119 @@
+// Device abstraction for the sigma_gb300 kernels.
+//
+// Every kernel is written as a per-item __host__ __device__ function plus a thin
+// grid-stride __global__ wrapper. The CUDA build launches the wrappers; the
+// serial emulation build (SIGMA_EMU, compiled by g++ for the CPU test suite only)
+// calls the item functions in a loop, so kernel logic can be checked without a
+// GPU. The product library is always the CUDA build.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+
+#if defined(__CUDACC__) && !defined(SIGMA_EMU)
+#define SIGMA_CUDA 1
+#include <cuda_runtime.h>
+#define HD __host__ __device__ __forceinline__
+#define DEV __device__ __forceinline__
+#else
+#define SIGMA_CUDA 0
+#define HD inline
+#define DEV inline
+#define __align__(n) alignas(n)
+#endif
+
+namespace sigma {
+
+typedef uint32_t u32;
+typedef uint64_t u64;
+typedef int64_t i64;
+
+// ---------------------------------------------------------------- atomics
+// Sequential emulation performs plain read-modify-writes.
+HD u32 atom_add(u32* p, u32 v) {
+#if defined(__CUDA_ARCH__)
+    return atomicAdd(p, v);
+#else
+    u32 o = *p; *p = o + v; return o;
+#endif
+}
+HD u64 atom_add64(u64* p, u64 v) {
+#if defined(__CUDA_ARCH__)
+    return (u64)atomicAdd((unsigned long long*)p, (unsigned long long)v);
+#else
+    u64 o = *p; *p = o + v; return o;
+#endif
+}
+HD u32 atom_min(u32* p, u32 v) {
+#if defined(__CUDA_ARCH__)
+    return atomicMin(p, v);
+#else
+    u32 o = *p; if (v < o) *p = v; return o;
+#endif
+}
+HD u64 atom_min64(u64* p, u64 v) {
+#if defined(__CUDA_ARCH__)
+    return (u64)atomicMin((unsigned long long*)p, (unsigned long long)v);
+#else
+    u64 o = *p; if (v < o) *p = v; return o;
+#endif
+}
+HD u32 atom_max(u32* p, u32 v) {
+#if defined(__CUDA_ARCH__)
+    return atomicMax(p, v);
+#else
+    u32 o = *p; if (v > o) *p = v; return o;
+#endif
+}
+HD u32 atom_cas(u32* p, u32 cmp, u32 v) {
+#if defined(__CUDA_ARCH__)
+    return atomicCAS(p, cmp, v);
+#else
+    u32 o = *p; if (o == cmp) *p = v; return o;
+#endif
+}
+HD u32 atom_or(u32* p, u32 v) {
+#if defined(__CUDA_ARCH__)
+    return atomicOr(p, v);
+#else
+    u32 o = *p; *p = o | v; return o;
+#endif
+}
+HD u32 atom_exch(u32* p, u32 v) {
+#if defined(__CUDA_ARCH__)
+    return atomicExch(p, v);
+#else
+    u32 o = *p; *p = v; return o;
+#endif
+}
+// Volatile load for values that other threads of the same launch may update.
+HD u32 vload(const u32* p) { return *(const volatile u32*)p; }
+
+HD int popc32(u32 x) {
+#if defined(__CUDA_ARCH__)
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
+}
+
+// Pair of words (usable in host and device code alike).
+struct U2 {
+    u32 x, y;
+};
+HD U2 mk_u2(u32 x, u32 y) { U2 r; r.x = x; r.y = y; return r; }
+
+// Error word bits (sticky per context; read back by the host after a stage).
+enum : u32 {
+    ERR_UNSAT = 1u << 0,        // a stage derived the empty clause
+    ERR_CAP_CLAUSES = 1u << 1,  // clause-slot capacity exceeded
+    ERR_CAP_LITS = 1u << 2,     // literal-pool capacity exceeded
+    ERR_CAP_WITNESS = 1u << 3,  // witness-stack capacity exceeded
+    ERR_CAP_SCRATCH = 1u << 4,  // per-variable scratch exceeded
+    ERR_ITER = 1u << 5,         // a bounded iteration gave up
+    ERR_INTERNAL = 1u << 6,     // invariant violated (bug)
+    ERR_INPUT = 1u << 7,        // invalid input formula
+};
+
+}  // namespace sigma

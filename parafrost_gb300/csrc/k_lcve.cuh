@@ -1,0 +1,112 @@
+// LCVE election: ParaFROST::LCVE + depFreeze (src/cpu/lcve.cpp:46-100), with the
+// variable order of varReorder (lcve.cpp:25-44, histogram.h:32-41, key.h:57-66).
+//
+// The reference walks candidates in (score, variable) order, skips eliminated,
+// zero-occurrence and frozen ones, stops at the first candidate whose two lists
+// reach the freezing temperatures (pt, nt), elects the rest and freezes every
+// neighbour v with ps[v] < pt or ns[v] < nt. Writing F for those freezable
+// variables, the elected set is the lexicographically-first independent set of
+// the co-occurrence graph restricted to F, in rank order, cut at the break
+// candidate B = the first valid candidate that is either outside F (it is never
+// frozen and its lists are necessarily long) or an independent-set member whose
+// lists reach the temperatures. The independent set is decided in parallel
+// rounds: a vertex joins when every lower-ranked neighbour is out, leaves when
+// one lower-ranked neighbour is in (Blelloch-Fineman-Shun deterministic greedy MIS).
+#pragma once
+
+#include "cnf.cuh"
+
+namespace sigma {
+
+enum : uint8_t { MIS_NONE = 0, MIS_UNDECIDED = 1, MIS_IN = 2, MIS_OUT = 3 };
+
+struct LcveArgs {
+    Ctx c;
+    u32 pt, nt;           // mu_pos << mu_inc, mu_neg << mu_inc
+    u32* score;           // nvars+1
+    u32* order;           // nvars: variables in (score, var) order
+    u32* rank;            // nvars+1
+    uint8_t* state;       // nvars+1
+    u32* bound;           // [0] = B0 (first valid non-F rank), [1] = B
+    u32* changed;         // round counter of undecided vertices
+    u32* pvs;             // elected variables in rank order
+};
+
+// write_scores (histogram.h:32-41): eligible[v-1] = v, scores[v] = ps*ns (32-bit wrap).
+HD void k_scores(const LcveArgs& a, u32 v) {
+    if (v == 0) return;
+    a.score[v] = a.c.ps[v] * a.c.ns[v];
+    a.order[v - 1] = v;
+}
+
+HD bool lcve_valid(const Ctx& c, u32 v) {
+    if (c.vstate[v]) return false;
+    return !(c.ps[v] == 0 && c.ns[v] == 0);
+}
+HD bool lcve_freezable(const LcveArgs& a, u32 v) { return a.c.ps[v] < a.pt || a.c.ns[v] < a.nt; }
+HD bool lcve_big(const LcveArgs& a, u32 v) {
+    return a.c.ot_size[V2L(v)] >= a.pt && a.c.ot_size[NEG(V2L(v))] >= a.nt;
+}
+
+// rank[v] and B0 = first valid candidate outside F.
+HD void k_rank(const LcveArgs& a, u32 p) {
+    const u32 v = a.order[p];
+    a.rank[v] = p;
+    if (lcve_valid(a.c, v) && !lcve_freezable(a, v)) atom_min(&a.bound[0], p);
+}
+
+HD void k_mis_init(const LcveArgs& a, u32 v) {
+    if (v == 0) { a.state[0] = MIS_NONE; return; }
+    const bool in_graph = lcve_valid(a.c, v) && lcve_freezable(a, v) && a.rank[v] < a.bound[0];
+    a.state[v] = in_graph ? MIS_UNDECIDED : MIS_NONE;
+}
+
+// One round for an undecided vertex v: scan its live clauses.
+HD void k_mis_round(const LcveArgs& a, u32 v) {
+    if (v == 0) return;
+    volatile uint8_t* st = (volatile uint8_t*)a.state;
+    if (st[v] != MIS_UNDECIDED) return;
+    const Ctx& c = a.c;
+    const u32 rv = a.rank[v];
+    bool pending = false;
+    for (u32 side = 0; side < 2; side++) {
+        const u32 l = V2L(v) + side;
+        const u32 o = c.ot_off[l], s = c.ot_size[l];
+        for (u32 i = 0; i < s; i++) {
+            const Hdr h = c.hdr[c.ot_refs[o + i]];
+            if (h_deleted(h.flags)) continue;
+            const u32* lits = c.lits + h.start;
+            for (u32 k = 0; k < h.size; k++) {
+                const u32 u = ABS(lits[k]);
+                if (u == v) continue;
+                const uint8_t su = st[u];
+                if (su == MIS_NONE || a.rank[u] > rv) continue;
+                if (su == MIS_IN) { st[v] = MIS_OUT; return; }
+                if (su == MIS_UNDECIDED) pending = true;
+            }
+        }
+    }
+    if (!pending) st[v] = MIS_IN;
+    else atom_add(a.changed, 1u);
+}
+
+// B = min(B0, first member whose lists reach the temperatures).
+HD void k_mis_bound(const LcveArgs& a, u32 v) {
+    if (v == 0) return;
+    if (a.state[v] == MIS_IN && lcve_big(a, v)) atom_min(&a.bound[1], a.rank[v]);
+}
+
+// Election flags over rank positions below B (compacted by the caller in rank order).
+HD void k_elect_flag(const LcveArgs& a, u32* flags, u32 p) {
+    const u32 v = a.order[p];
+    flags[p] = (p < a.bound[1] && a.state[v] == MIS_IN) ? 1u : 0u;
+}
+
+HD void k_elect_write(const LcveArgs& a, const u32* flags, const u32* scan, u32 p) {
+    if (!flags[p]) return;
+    const u32 v = a.order[p];
+    a.pvs[scan[p]] = v;
+    a.c.pvrank[v] = scan[p];
+}
+
+}  // namespace sigma

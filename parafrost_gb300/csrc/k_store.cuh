@@ -1,0 +1,127 @@
+// Clause-store kernels: upload normalisation, occurrence-table build, survivor
+// counts and compaction. Item functions run once per clause / literal slot.
+#pragma once
+
+#include "cnf.cuh"
+#include "introsort.cuh"
+
+namespace sigma {
+
+// ---------------------------------------------------------------- upload
+// extract() (src/cpu/simplify.cpp:95-113; GPU: transfer.cu:24-42 + prep_cnf_k,
+// kernels.cu:61-70): literals sorted ascending, signature over the clause,
+// status from the learnt flag. Rejects literals out of range and clauses that
+// repeat a variable.
+struct UploadArgs {
+    Ctx c;
+    const u64* off;      // num_clauses + 1
+    const uint8_t* learnt;  // may be null
+    u64 base;            // literal offset of off[0]
+};
+
+HD void k_upload_clause(const UploadArgs& a, u32 i) {
+    const u64 s = a.off[i] - a.base, e = a.off[i + 1] - a.base;
+    u32* l = a.c.lits + s;
+    const u32 n = (u32)(e - s);
+    if (n == 0) { set_err(a.c, ERR_INPUT); return; }
+    if (n <= 32) ref_insertion_sort(l, (int)n, LitLess());
+    else std_sort_replica(l, l + n, LitLess());
+    u32 sig = 0;
+    for (u32 k = 0; k < n; k++) {
+        const u32 lit = l[k];
+        if (lit < 2 || lit >= a.c.D) { set_err(a.c, ERR_INPUT); return; }
+        if (k && ABS(lit) == ABS(l[k - 1])) { set_err(a.c, ERR_INPUT); return; }
+        sig |= MAPHASH(lit);
+    }
+    Hdr h;
+    h.start = (u32)s;
+    h.size = n;
+    h.sig = sig;
+    h.flags = (a.learnt && a.learnt[i]) ? ST_LEARNT : ST_ORIGINAL;
+    a.c.hdr[i] = h;
+}
+
+// ---------------------------------------------------------------- OT build
+// createOT (src/cpu/simplify.cpp:35-56) as histogram -> exclusive scan -> scatter
+// (GPU reference: histogram.cu:34-52, memory.cu:271-312, create_ot_k kernels.cu:81-96).
+HD void k_hist_clause(const Ctx& c, u32 i) {
+    const Hdr h = c.hdr[i];
+    if (h_deleted(h.flags)) return;
+    const u32* l = c.lits + h.start;
+    for (u32 k = 0; k < h.size; k++) atom_add(&c.ot_size[l[k]], 1u);
+}
+
+HD void k_scatter_clause(const Ctx& c, u32 i) {
+    const Hdr h = c.hdr[i];
+    if (h_deleted(h.flags)) return;
+    const u32* l = c.lits + h.start;
+    for (u32 k = 0; k < h.size; k++) {
+        const u32 pos = atom_add(&c.ot_cursor[l[k]], 1u);
+        if (pos < c.ot_cap) c.ot_refs[pos] = i;
+        else set_err(c, ERR_INTERNAL);
+    }
+}
+
+// occurs[v] = (ps, ns) over live clauses (histSimp, src/cpu/histogram.cpp:82-96).
+HD void k_occurs_clause(const Ctx& c, u32 i) {
+    const Hdr h = c.hdr[i];
+    if (h_deleted(h.flags)) return;
+    const u32* l = c.lits + h.start;
+    for (u32 k = 0; k < h.size; k++) {
+        const u32 lit = l[k];
+        atom_add(SIGN(lit) ? &c.ns[ABS(lit)] : &c.ps[ABS(lit)], 1u);
+    }
+}
+
+// occurs straight from the occurrence-list sizes (valid when no clause changed since
+// the OT build): ps = |ot[2v]|, ns = |ot[2v+1]|.
+HD void k_occurs_from_ot(const Ctx& c, u32 v) {
+    if (v == 0) { c.ps[0] = c.ns[0] = 0; return; }
+    c.ps[v] = c.ot_size[V2L(v)];
+    c.ns[v] = c.ot_size[NEG(V2L(v))];
+}
+
+// ---------------------------------------------------------------- counts
+// countAll (src/cpu/solve.h:724-734): live clauses and their literals.
+struct CountArgs {
+    Ctx c;
+    u64* out;  // [0] clauses, [1] literals
+};
+HD void k_count_clause(const CountArgs& a, u32 i) {
+    const Hdr h = a.c.hdr[i];
+    if (h_deleted(h.flags)) return;
+    atom_add64(&a.out[0], 1ull);
+    atom_add64(&a.out[1], (u64)h.size);
+}
+
+// ---------------------------------------------------------------- compaction
+// shrinkSimp (src/cpu/simplify.cpp:234-245; GPU: recycle.cu:30-97): drop deleted
+// clauses, keep order. Two exclusive scans (kept clauses, kept literals) give the
+// new id and the new literal start of every survivor.
+struct GcArgs {
+    Ctx c;
+    const u32* keep_scan;    // exclusive scan of keep flags
+    const u64* lit_scan;     // exclusive scan of kept sizes
+    Hdr* new_hdr;
+    u32* new_lits;
+};
+HD void k_gc_flags(const Ctx& c, u32* keep, u64* sizes, u32 i) {
+    const Hdr h = c.hdr[i];
+    const bool k = !h_deleted(h.flags);
+    keep[i] = k ? 1u : 0u;
+    sizes[i] = k ? (u64)h.size : 0ull;
+}
+HD void k_gc_move(const GcArgs& a, u32 i) {
+    const Hdr h = a.c.hdr[i];
+    if (h_deleted(h.flags)) return;
+    const u32 id = a.keep_scan[i];
+    const u64 st = a.lit_scan[i];
+    Hdr nh = h;
+    nh.start = (u32)st;
+    a.new_hdr[id] = nh;
+    const u32* src = a.c.lits + h.start;
+    u32* dst = a.new_lits + st;
+    for (u32 k = 0; k < h.size; k++) dst[k] = src[k];
+}
+
+}  // namespace sigma

@@ -1,0 +1,1077 @@
+// sigma_gb300 host driver: one context = one resident formula. Implements the
+// C ABI of include/sigma_gb300.h and runs ParaFROST's sigmify round
+// (ParaFROST::sigmifying, src/cpu/simplify.cpp:157-232; GPU twin
+// src/gpu/simplify.cu:155-234) as a sequence of device stages.
+#include "../../include/sigma_gb300.h"
+
+#include "cnf.cuh"
+#include "k_bce_ere.cuh"
+#include "k_bve.cuh"
+#include "k_lcve.cuh"
+#include "k_prop.cuh"
+#include "k_sortot.cuh"
+#include "k_store.cuh"
+#include "k_sub.cuh"
+#include "prims.cuh"
+#include "runtime.h"
+
+#include <algorithm>
+#include <climits>
+#include <map>
+#include <set>
+#include <vector>
+
+using namespace sigma;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+// ---------------------------------------------------------------- functors
+struct FUpload { UploadArgs a; HD void operator()(u32 i) const { k_upload_clause(a, i); } };
+struct FHist { Ctx c; HD void operator()(u32 i) const { k_hist_clause(c, i); } };
+struct FScatter { Ctx c; HD void operator()(u32 i) const { k_scatter_clause(c, i); } };
+struct FOccursCl { Ctx c; HD void operator()(u32 i) const { k_occurs_clause(c, i); } };
+struct FOccursOt { Ctx c; HD void operator()(u32 i) const { k_occurs_from_ot(c, i); } };
+struct FCount { CountArgs a; HD void operator()(u32 i) const { k_count_clause(a, i); } };
+struct FGcFlags { Ctx c; u32* keep; u64* sizes; HD void operator()(u32 i) const { k_gc_flags(c, keep, sizes, i); } };
+struct FGcMove { GcArgs a; HD void operator()(u32 i) const { k_gc_move(a, i); } };
+struct FPropLists { PropArgs a; HD void operator()(u32 i) const { k_prop_lists(a, i); } };
+struct FPropClause { PropArgs a; HD void operator()(u32 i) const { k_prop_clause(a, i); } };
+struct FReduce { Ctx c; HD void operator()(u32 i) const { k_reduce_list(c, i); } };
+struct FScores { LcveArgs a; HD void operator()(u32 i) const { k_scores(a, i); } };
+struct FRank { LcveArgs a; HD void operator()(u32 i) const { k_rank(a, i); } };
+struct FMisInit { LcveArgs a; HD void operator()(u32 i) const { k_mis_init(a, i); } };
+struct FMisRound { LcveArgs a; HD void operator()(u32 i) const { k_mis_round(a, i); } };
+struct FMisBound { LcveArgs a; HD void operator()(u32 i) const { k_mis_bound(a, i); } };
+struct FElectFlag { LcveArgs a; u32* flags; HD void operator()(u32 i) const { k_elect_flag(a, flags, i); } };
+struct FElectWrite { LcveArgs a; const u32* flags; const u32* scan; HD void operator()(u32 i) const { k_elect_write(a, flags, scan, i); } };
+struct FFill32 { u32* p; u32 v; HD void operator()(u32 i) const { p[i] = v; } };
+struct FSortList { SortArgs a; HD void operator()(u32 i) const { k_sort_list(a, i); } };
+struct FSubPossible { SubArgs a; u32* flag; HD void operator()(u32 i) const { k_sub_unit_possible(a, flag, i); } };
+struct FSubPv { SubArgs a; HD void operator()(u32 i) const { k_sub_pv(a, i); } };
+struct FSubNeed { Ctx c; const u32* pvs; u32* ent; u64* words; HD void operator()(u32 i) const { k_sub_need(c, pvs, ent, words, i); } };
+struct FSubSave { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_save(a, i); } };
+struct FSubRestore { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_restore(a, i); } };
+struct FSubReach { SubReachArgs a; HD void operator()(u32 i) const { k_sub_reach(a, i); } };
+struct FSubCommit { Ctx c; const u32* lits; HD void operator()(u32 i) const { k_sub_commit_oblivion(c, lits, i); } };
+struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) const { k_bve_scratch_need(c, pvs, need, i); } };
+struct FBveAnalyze { BveArgs a; HD void operator()(u32 i) const { k_bve_analyze(a, i); } };
+struct FBveWrite { BveArgs a; HD void operator()(u32 i) const { k_bve_write(a, i); } };
+struct FBceCount { BceArgs a; HD void operator()(u32 i) const { k_bce_count(a, i); } };
+struct FBceWrite { BceArgs a; HD void operator()(u32 i) const { k_bce_write(a, i); } };
+struct FEre { EreArgs a; HD void operator()(u32 i) const { k_ere_pv(a, i); } };
+struct FEreResolve { EreArgs a; HD void operator()(u32 i) const { k_ere_resolve(a, i); } };
+struct FEreFix { EreArgs a; const u64* keys; u32 n; HD void operator()() const { ere_fixup(a, keys, n); } };
+struct FEreSeq { EreArgs a; HD void operator()() const { ere_sequential(a); } };
+// per-PV working set in bytes (roofline accounting): 4*occ + sum(8 + 4*len)
+struct FPvBytes {
+    Ctx c; const u32* pvs; u64* out;
+    HD void operator()(u32 k) const {
+        const u32 p = V2L(pvs[k]);
+        u64 b = 0;
+        for (u32 side = 0; side < 2; side++) {
+            const u32 l = p + side, o = c.ot_off[l], s = c.ot_size[l];
+            b += 4ull * s;
+            for (u32 i = 0; i < s; i++) b += 8ull + 4ull * c.hdr[c.ot_refs[o + i]].size;
+        }
+        atom_add64(out, b);
+    }
+};
+
+enum Stage { ST_OT = 0, ST_PROP, ST_LCVE, ST_SORT, ST_SUB, ST_VE, ST_BCE, ST_ERE, ST_GC, ST_COUNT, ST_UP, ST_DOWN };
+
+}  // namespace
+
+struct pf_sigma_ctx {
+    pf_options opt;
+    Runtime rt;
+    StageTimer tm;
+    bool uploaded = false, has_learnt = false;
+    u32 nvars = 0, D = 0;
+    u32 ncls = 0;
+    u64 nlits_used = 0;
+    u32 ntrail = 0, prop_head = 0;
+    u64 nresolved = 0;
+    u32 wave_stamp = 0;
+    // clause store (double-buffered for compaction)
+    DBuf<Hdr> hdr, hdr2;
+    DBuf<u32> lits, lits2;
+    // occurrence table
+    DBuf<u32> ot_off, ot_size, ot_refs, ot_cursor;
+    // variables
+    DBuf<u32> asg, ps, ns, pvrank;
+    DBuf<uint8_t> vstate;
+    DBuf<u32> trail, resolved;
+    DBuf<u32> counters;   // [0] ntrail, [1] err, [2..] scratch counters
+    DBuf<u64> counters64; // [0] nresolved, [1..] scratch
+    // stage scratch
+    DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
+    DBuf<uint8_t> mis_state;
+    DBuf<u32> work, cl_stamp;
+    DBuf<u32> radix_hist, radix_hscan, scan_tmp32;
+    DBuf<u64> scan_tmp64;
+    DBuf<u64> big64a, big64b;
+    DBuf<u32> big32a, big32b;
+    // BVE
+    DBuf<uint8_t> ve_type;
+    DBuf<u32> ve_porgs, ve_norgs, ve_ncls, ve_nlits, ve_nwit, ve_def, ve_cls_scan, ve_scr;
+    DBuf<u64> ve_scr_off, ve_lit_scan, ve_wit_scan;
+    // SUB safe path
+    DBuf<U2> sub_units, sub_pairs;
+    DBuf<u32> sub_ent, sub_ent_off, sub_ids, sub_words, sub_sizes, sub_pre_off, sub_pre_lits, sub_ulits;
+    DBuf<u64> sub_wrd, sub_wrd_off;
+    DBuf<Hdr> sub_hdrs;
+    DBuf<uint8_t> sub_run;
+    // ERE
+    DBuf<u64> ere_claim, ere_key;
+    DBuf<u32> ere_target, ere_losers;
+    // host state
+    u32 npvs = 0;
+    bool ot_dirty = false;  // clauses changed since the OT build
+    int phase = 0;
+    u32 mu_inc = 0;
+    i64 n_cls_after = 0, n_lits_after = 0;
+    pf_round_stats st;
+    std::vector<uint32_t> dump;
+    u64 alg_bytes = 0;
+
+    Ctx view() {
+        Ctx c;
+        c.nvars = nvars;
+        c.D = D;
+        c.hdr = hdr.p;
+        c.lits = lits.p;
+        c.ncls = ncls;
+        c.cap_cls = (u32)hdr.n;
+        c.nlits_used = nlits_used;
+        c.cap_lits = lits.n;
+        c.ot_off = ot_off.p;
+        c.ot_size = ot_size.p;
+        c.ot_refs = ot_refs.p;
+        c.ot_cursor = ot_cursor.p;
+        c.ot_cap = (u32)ot_refs.n;
+        c.asg = asg.p;
+        c.vstate = vstate.p;
+        c.ps = ps.p;
+        c.ns = ns.p;
+        c.pvrank = pvrank.p;
+        c.trail = trail.p;
+        c.ntrail = counters.p + 0;
+        c.resolved = resolved.p;
+        c.nresolved = counters64.p + 0;
+        c.cap_resolved = resolved.n;
+        c.err = counters.p + 1;
+        return c;
+    }
+
+    u32 read_err() {
+        u32 e = 0;
+        rt.d2h(&e, counters.p + 1, 4);
+        return e;
+    }
+    u32 read_u32(const u32* d) {
+        u32 v = 0;
+        rt.d2h(&v, d, 4);
+        return v;
+    }
+    u64 read_u64(const u64* d) {
+        u64 v = 0;
+        rt.d2h(&v, d, 8);
+        return v;
+    }
+    void write_u32(u32* d, u32 v) { rt.h2d(d, &v, 4); }
+    void write_u64(u64* d, u64 v) { rt.h2d(d, &v, 8); }
+
+    // exclusive scans
+    u32 scan32(const u32* in, u32* out, size_t n) {
+        scan_tmp32.reserve(rt, scan_tmp_elems(n) + 2);
+        u32* total = scan_tmp32.p + scan_tmp32.n - 1;
+        excl_scan<u32, u32>(in, out, n, total, scan_tmp32.p, rt.stream);
+        return read_u32(total);
+    }
+    template <class Tin>
+    u64 scan64(const Tin* in, u64* out, size_t n) {
+        scan_tmp64.reserve(rt, scan_tmp_elems(n) + 2);
+        u64* total = scan_tmp64.p + scan_tmp64.n - 1;
+        excl_scan<Tin, u64>(in, out, n, total, scan_tmp64.p, rt.stream);
+        return read_u64(total);
+    }
+
+    // ------------------------------------------------------------ dumps
+    void rec(u32 kind, u32 ph, u32 stage, const std::vector<u32>& d) {
+        dump.push_back(kind);
+        dump.push_back(ph);
+        dump.push_back(stage);
+        dump.push_back((u32)d.size());
+        dump.insert(dump.end(), d.begin(), d.end());
+    }
+    template <class T>
+    std::vector<T> fetch(const T* d, size_t n) {
+        std::vector<T> h(n);
+        if (n) rt.d2h(h.data(), d, n * sizeof(T));
+        return h;
+    }
+    void dump_cnf(u32 ph, u32 stage) {
+        auto H = fetch(hdr.p, ncls);
+        auto L = fetch(lits.p, nlits_used);
+        std::vector<u32> d;
+        d.push_back(ncls);
+        for (u32 i = 0; i < ncls; i++) {
+            d.push_back(H[i].flags & 15u);
+            d.push_back(H[i].sig);
+            d.push_back(H[i].size);
+            for (u32 k = 0; k < H[i].size; k++) d.push_back(L[H[i].start + k]);
+        }
+        rec(1, ph, stage, d);
+    }
+    void dump_trail(u32 ph, u32 stage) { rec(7, ph, stage, fetch(trail.p, ntrail)); }
+    void dump_resolved(u32 ph, u32 stage) { rec(8, ph, stage, fetch(resolved.p, nresolved)); }
+    void dump_elim(u32 ph, u32 stage) {
+        auto vs = fetch(vstate.p, nvars + 1);
+        std::vector<u32> d;
+        for (u32 v = 1; v <= nvars; v++) if (vs[v]) d.push_back(v);
+        rec(9, ph, stage, d);
+    }
+    void dump_stage(u32 ph, u32 stage) {
+        if (opt.dump_level < 2) return;
+        dump_cnf(ph, stage);
+        dump_trail(ph, stage);
+        if (stage >= 5) dump_resolved(ph, stage);
+    }
+    void dump_pvlists(u32 ph) {
+        auto P = fetch(pvs.p, npvs);
+        auto off = fetch(ot_off.p, D + 1);
+        auto sz = fetch(ot_size.p, D);
+        auto refs = fetch(ot_refs.p, off[D]);
+        std::vector<u32> d;
+        for (u32 v : P) {
+            for (u32 l = V2L(v); l <= V2L(v) + 1; l++) {
+                d.push_back(sz[l]);
+                for (u32 i = 0; i < sz[l]; i++) d.push_back(refs[off[l] + i]);
+            }
+        }
+        rec(6, ph, 3, d);
+    }
+
+    void check(u32 stage_err_mask = ~0u) {
+        const u32 e = read_err() & stage_err_mask;
+        if (e & ERR_UNSAT) throw int(PF_UNSAT);
+        if (e & (ERR_CAP_CLAUSES | ERR_CAP_LITS | ERR_CAP_WITNESS | ERR_CAP_SCRATCH)) throw std::runtime_error("capacity exceeded (internal sizing bug)");
+        if (e & ERR_ITER) throw int(PF_ETIMEOUT);
+        if (e & ERR_INPUT) throw int(PF_EINVAL);
+        if (e & ERR_INTERNAL) throw std::runtime_error("internal invariant violated");
+    }
+
+    // ------------------------------------------------------------ capacity
+    void ensure_clauses(u64 need) {
+        if (need <= hdr.n) return;
+        const size_t cap = (size_t)(need + need / 4 + 1024);
+        if (cap > 0xFFFFFFF0ull) throw OomError("clause count exceeds 32-bit ids");
+        hdr.grow(rt, cap, ncls);
+    }
+    void ensure_lits(u64 need) {
+        if (need <= lits.n) return;
+        const size_t cap = (size_t)(need + need / 4 + 4096);
+        if (cap > 0xFFFFFFF0ull) throw OomError("literal pool exceeds 32-bit offsets");
+        lits.grow(rt, cap, nlits_used);
+    }
+    void ensure_resolved(u64 need) {
+        if (need <= resolved.n) return;
+        resolved.grow(rt, (size_t)(need + need / 4 + 4096), nresolved);
+    }
+
+    // ------------------------------------------------------------ stages
+    // createOT (simplify.cpp:35-56).
+    void create_ot() {
+        Ctx c = view();
+        rt.zero(ot_size.p, (size_t)D * 4);
+        rt.each(FHist{c}, ncls);
+        const u32 total = scan32(ot_size.p, ot_off.p, D);
+        write_u32(ot_off.p + D, total);
+        if (total > ot_refs.n) ot_refs.reserve(rt, (size_t)total + total / 4 + 1024);
+        rt.d2d(ot_cursor.p, ot_off.p, (size_t)D * 4);
+        c = view();
+        rt.each(FScatter{c}, ncls);
+        check();
+        ot_dirty = false;
+        alg_bytes += 2ull * (4ull * nlits_used + 8ull * ncls) + 8ull * D + 4ull * total;
+    }
+
+    // prop (elimination.cpp:64-99).
+    void prop() {
+        if (prop_head >= ntrail) return;
+        work.reserve(rt, (size_t)std::max<u64>(ot_refs.n, 1024));
+        if (cl_stamp.n < hdr.n) {
+            cl_stamp.reserve(rt, hdr.n);
+            rt.zero(cl_stamp.p, cl_stamp.bytes());
+            wave_stamp = 0;
+        }
+        u32 guard = 0;
+        while (prop_head < ntrail) {
+            if (++guard > nvars + 2) throw int(PF_ETIMEOUT);
+            const u32 pend = ntrail - prop_head;
+            PropArgs a;
+            a.c = view();
+            a.head = prop_head;
+            a.stamp = ++wave_stamp;
+            a.cl_stamp = cl_stamp.p;
+            a.work = work.p;
+            a.nwork = counters.p + 2;
+            a.cap_work = (u32)work.n;
+            write_u32(counters.p + 2, 0);
+            rt.each(FPropLists{a}, pend);
+            const u32 nw = read_u32(counters.p + 2);
+            prop_head = ntrail;
+            rt.each(FPropClause{a}, nw);
+            ntrail = read_u32(counters.p + 0);
+            check();
+        }
+        ot_dirty = true;
+        if (!opt.sub) rt.each(FReduce{view()}, D);
+    }
+
+    // LCVE (lcve.cpp:46-81).
+    bool lcve() {
+        Ctx c = view();
+        rt.zero(ps.p, (size_t)(nvars + 1) * 4);
+        rt.zero(ns.p, (size_t)(nvars + 1) * 4);
+        if (ot_dirty) rt.each(FOccursCl{c}, ncls);
+        else rt.each(FOccursOt{c}, nvars + 1);
+        LcveArgs a;
+        a.c = c;
+        a.pt = (u32)opt.mu_pos << mu_inc;
+        a.nt = (u32)opt.mu_neg << mu_inc;
+        a.score = score.p;
+        a.order = order.p;
+        a.rank = rank.p;
+        a.state = mis_state.p;
+        a.bound = bound.p;
+        a.changed = counters.p + 3;
+        a.pvs = pvs.p;
+        rt.zero(score.p, (size_t)(nvars + 1) * 4);
+        rt.each(FScores{a}, nvars + 1);
+        // LCV order: stable by score over ascending variables (rSort, sort.h:123-133)
+        rt.d2d(order_k2.p, score.p + 1, (size_t)nvars * 4);  // keys = score[1..]
+        radix_sort_pairs(order_k2.p, order.p, order_v2.p, rank.p, nvars, 32, radix_hist.p, radix_hscan.p,
+                         scan_tmp32.p, rt.stream);
+        u32 init_b[2] = {NONE, NONE};
+        rt.h2d(bound.p, init_b, 8);
+        rt.each(FRank{a}, nvars);
+        rt.each(FMisInit{a}, nvars + 1);
+        u32 rounds = 0;
+        while (true) {
+            if (++rounds > nvars + 2) throw int(PF_ETIMEOUT);
+            write_u32(counters.p + 3, 0);
+            rt.each(FMisRound{a}, nvars + 1);
+            if (read_u32(counters.p + 3) == 0) break;
+        }
+        rt.d2d(bound.p + 1, bound.p, 4);
+        rt.each(FMisBound{a}, nvars + 1);
+        rt.each(FFill32{pvrank.p, NONE}, nvars + 1);
+        rt.each(FElectFlag{a, flags.p}, nvars);
+        npvs = scan32(flags.p, flags_scan.p, nvars);
+        rt.each(FElectWrite{a, flags.p, flags_scan.p}, nvars);
+        alg_bytes += 4ull * D + 24ull * nvars;
+        if (opt.dump_level >= 2) {
+            rec(3, phase, 2, fetch(score.p, nvars + 1));
+            rec(4, phase, 2, fetch(order.p, nvars));
+        }
+        if (opt.dump_level >= 1) rec(5, phase, 2, fetch(pvs.p, npvs));
+        return npvs >= (u32)opt.lcve_min;
+    }
+
+    void sort_ot() {
+        SortArgs a{view(), pvs.p};
+        rt.each(FSortList{a}, 2 * npvs);
+    }
+
+    u64 pv_bytes() {
+        rt.zero(counters64.p + 1, 8);
+        rt.each(FPvBytes{view(), pvs.p, counters64.p + 1}, npvs);
+        return read_u64(counters64.p + 1);
+    }
+
+    // SUB (elimination.cpp:110-129).
+    void sub() {
+        if (!(opt.sub || opt.ve_plus) || !npvs) return;
+        SubArgs a;
+        a.c = view();
+        a.pvs = pvs.p;
+        a.npvs = npvs;
+        a.sub_max = (u32)opt.sub_max;
+        a.units = nullptr;
+        a.nunits = counters.p + 4;
+        a.cap_units = 0;
+        a.pre_off = nullptr;
+        a.pre_lits = nullptr;
+        a.run = nullptr;
+        write_u32(counters.p + 5, 0);
+        rt.each(FSubPossible{a, counters.p + 5}, npvs);
+        if (read_u32(counters.p + 5) == 0) {
+            rt.each(FSubPv{a}, npvs);
+            check();
+            return;
+        }
+        sub_safe(a);
+    }
+
+    void sub_safe(SubArgs a) {
+        Ctx c = view();
+        // checkpoint
+        sub_ent.reserve(rt, npvs + 1);
+        sub_ent_off.reserve(rt, npvs + 1);
+        sub_wrd.reserve(rt, npvs + 1);
+        sub_wrd_off.reserve(rt, npvs + 1);
+        rt.each(FSubNeed{c, pvs.p, sub_ent.p, sub_wrd.p}, npvs);
+        const u32 ents = scan32(sub_ent.p, sub_ent_off.p, npvs);
+        const u64 words = scan64(sub_wrd.p, sub_wrd_off.p, npvs);
+        sub_ids.reserve(rt, ents + 1);
+        sub_hdrs.reserve(rt, ents + 1);
+        sub_words.reserve(rt, (size_t)words + 1);
+        sub_sizes.reserve(rt, 2 * npvs + 2);
+        SubCkptArgs ck{c, pvs.p, sub_ent_off.p, sub_wrd_off.p, sub_ids.p, sub_hdrs.p, sub_words.p, sub_sizes.p, nullptr};
+        rt.each(FSubSave{ck}, npvs);
+        // first pass
+        sub_units.reserve(rt, (size_t)ents + 16);
+        a.units = sub_units.p;
+        a.cap_units = (u32)sub_units.n;
+        write_u32(counters.p + 4, 0);
+        rt.each(FSubPv{a}, npvs);
+        check();
+        u32 nu = read_u32(counters.p + 4);
+        if (nu == 0) return;
+        // host bookkeeping: units per producer, used pre-deletions per PV
+        std::vector<U2> units = fetch(sub_units.p, nu);
+        std::map<u32, std::vector<u32>> used;  // PV rank -> literals pre-deleted in its last run
+        sub_run.reserve(rt, npvs);
+        for (int iter = 0;; iter++) {
+            if (iter > (int)npvs + 2) throw int(PF_ETIMEOUT);
+            // reach pairs from the current units
+            std::sort(units.begin(), units.end(), [](const U2& x, const U2& y) { return x.x < y.x; });
+            sub_ulits.reserve(rt, units.size() + 1);
+            sub_units.reserve(rt, std::max<size_t>(units.size(), 16));
+            rt.h2d(sub_units.p, units.data(), units.size() * sizeof(U2));
+            const size_t cap_pairs = 1 << 20;
+            sub_pairs.reserve(rt, cap_pairs);
+            write_u32(counters.p + 6, 0);
+            SubReachArgs ra{view(), sub_units.p, sub_pairs.p, counters.p + 6, (u32)cap_pairs};
+            rt.each(FSubReach{ra}, (u32)units.size());
+            check();
+            const u32 np = read_u32(counters.p + 6);
+            std::vector<U2> pairs = fetch(sub_pairs.p, np);
+            std::map<u32, std::vector<u32>> want;
+            for (const U2& pr : pairs) want[pr.x].push_back(units[pr.y].y);
+            for (auto& kv : want) {
+                std::sort(kv.second.begin(), kv.second.end());
+                kv.second.erase(std::unique(kv.second.begin(), kv.second.end()), kv.second.end());
+            }
+            // PVs whose pre-deleted set changed
+            std::vector<u32> rerun;
+            std::set<u32> keys;
+            for (auto& kv : want) keys.insert(kv.first);
+            for (auto& kv : used) keys.insert(kv.first);
+            for (u32 k : keys) {
+                const auto w = want.count(k) ? want[k] : std::vector<u32>();
+                const auto u = used.count(k) ? used[k] : std::vector<u32>();
+                if (w != u) rerun.push_back(k);
+            }
+            if (rerun.empty()) break;
+            // restore and re-run them with their pre-deletions
+            std::vector<uint8_t> run(npvs, 0);
+            for (u32 k : rerun) run[k] = 1;
+            rt.h2d(sub_run.p, run.data(), npvs);
+            SubCkptArgs rk = ck;
+            rk.c = view();
+            rk.run = sub_run.p;
+            rt.each(FSubRestore{rk}, npvs);
+            std::vector<u32> poff(npvs + 1, 0), plits;
+            for (u32 k = 0; k < npvs; k++) {
+                poff[k] = (u32)plits.size();
+                if (run[k] && want.count(k)) plits.insert(plits.end(), want[k].begin(), want[k].end());
+            }
+            poff[npvs] = (u32)plits.size();
+            sub_pre_off.reserve(rt, npvs + 1);
+            sub_pre_lits.reserve(rt, plits.size() + 1);
+            rt.h2d(sub_pre_off.p, poff.data(), poff.size() * 4);
+            rt.h2d(sub_pre_lits.p, plits.data(), plits.size() * 4);
+            for (u32 k : rerun) {
+                if (want.count(k)) used[k] = want[k];
+                else used.erase(k);
+            }
+            // drop the re-run PVs' old units, collect their new ones
+            std::vector<U2> kept;
+            for (const U2& u : units) if (!run[u.x]) kept.push_back(u);
+            sub_units.reserve(rt, (size_t)ents + 16);
+            SubArgs b = a;
+            b.c = view();
+            b.units = sub_units.p;
+            b.cap_units = (u32)sub_units.n;
+            b.pre_off = sub_pre_off.p;
+            b.pre_lits = sub_pre_lits.p;
+            b.run = sub_run.p;
+            write_u32(counters.p + 4, 0);
+            rt.each(FSubPv{b}, npvs);
+            check();
+            const u32 nn = read_u32(counters.p + 4);
+            std::vector<U2> fresh = fetch(sub_units.p, nn);
+            kept.insert(kept.end(), fresh.begin(), fresh.end());
+            units.swap(kept);
+        }
+        // commit in producer order: enqueueUnit + toblivion(ot[unit])
+        std::stable_sort(units.begin(), units.end(), [](const U2& x, const U2& y) { return x.x < y.x; });
+        std::vector<u32> A = fetch(asg.p, nvars + 1);
+        std::vector<u32> tr, ul;
+        for (const U2& u : units) {
+            const u32 lit = u.y, v = ABS(lit);
+            if (A[v] == 0) { A[v] = lit; tr.push_back(lit); ul.push_back(lit); }
+            else if (A[v] != lit) throw int(PF_UNSAT);
+        }
+        for (u32 lit : tr) write_u32(asg.p + ABS(lit), lit);
+        if (!tr.empty()) {
+            rt.h2d(trail.p + ntrail, tr.data(), tr.size() * 4);
+            ntrail += (u32)tr.size();
+            write_u32(counters.p + 0, ntrail);
+            sub_ulits.reserve(rt, ul.size() + 1);
+            rt.h2d(sub_ulits.p, ul.data(), ul.size() * 4);
+            rt.each(FSubCommit{view(), sub_ulits.p}, (u32)ul.size());
+        }
+    }
+
+    // VE (elimination.cpp:101-108) = bve (bve.cpp:28-142).
+    void ve() {
+        if (!opt.ve || !npvs) return;
+        Ctx c = view();
+        ve_type.reserve(rt, npvs);
+        ve_porgs.reserve(rt, npvs);
+        ve_norgs.reserve(rt, npvs);
+        ve_ncls.reserve(rt, npvs);
+        ve_nlits.reserve(rt, npvs);
+        ve_nwit.reserve(rt, npvs);
+        ve_def.reserve(rt, npvs);
+        ve_cls_scan.reserve(rt, npvs);
+        ve_scr_off.reserve(rt, npvs + 1);
+        ve_lit_scan.reserve(rt, npvs);
+        ve_wit_scan.reserve(rt, npvs);
+        big64a.reserve(rt, npvs + 1);
+        rt.each(FBveNeed{c, pvs.p, big64a.p}, npvs);
+        const u64 scr_words = scan64(big64a.p, ve_scr_off.p, npvs);
+        ve_scr.reserve(rt, (size_t)scr_words + 16);
+        BveArgs a;
+        a.c = c;
+        a.pvs = pvs.p;
+        a.npvs = npvs;
+        a.ve_clause_max = opt.ve_clause_max;
+        a.ve_lbound = opt.ve_lbound;
+        a.xor_max_arity = opt.xor_max_arity;
+        a.type = ve_type.p;
+        a.porgs = ve_porgs.p;
+        a.norgs = ve_norgs.p;
+        a.ncls = ve_ncls.p;
+        a.nlits = ve_nlits.p;
+        a.nwit = ve_nwit.p;
+        a.def = ve_def.p;
+        a.scr_off = ve_scr_off.p;
+        a.scr = ve_scr.p;
+        rt.each(FBveAnalyze{a}, npvs);
+        check();
+        const u32 add_cls = scan32(ve_ncls.p, ve_cls_scan.p, npvs);
+        const u64 add_lits = scan64(ve_nlits.p, ve_lit_scan.p, npvs);
+        const u64 add_wit = scan64(ve_nwit.p, ve_wit_scan.p, npvs);
+        ensure_clauses((u64)ncls + add_cls);
+        ensure_lits(nlits_used + add_lits);
+        ensure_resolved(nresolved + add_wit);
+        a.c = view();
+        a.cls_scan = ve_cls_scan.p;
+        a.lit_scan = ve_lit_scan.p;
+        a.wit_scan = ve_wit_scan.p;
+        a.cls_base = ncls;
+        a.lit_base = nlits_used;
+        a.wit_base = nresolved;
+        rt.each(FBveWrite{a}, npvs);
+        ncls += add_cls;
+        nlits_used += add_lits;
+        nresolved += add_wit;
+        ntrail = read_u32(counters.p + 0);
+        check();
+        alg_bytes += 4ull * add_lits + 8ull * add_cls + 4ull * add_wit;
+    }
+
+    // BCE (elimination.cpp:131-167).
+    void bce() {
+        if (!opt.bce || !npvs) return;
+        BceArgs a;
+        a.c = view();
+        a.pvs = pvs.p;
+        a.bce_max = (u32)opt.bce_max;
+        ve_nwit.reserve(rt, npvs);
+        ve_wit_scan.reserve(rt, npvs);
+        a.nwit = ve_nwit.p;
+        rt.each(FBceCount{a}, npvs);
+        const u64 add = scan64(ve_nwit.p, ve_wit_scan.p, npvs);
+        if (!add) return;
+        ensure_resolved(nresolved + add);
+        a.c = view();
+        a.wit_scan = ve_wit_scan.p;
+        a.wit_base = nresolved;
+        rt.each(FBceWrite{a}, npvs);
+        nresolved += add;
+        alg_bytes += 4ull * add;
+    }
+
+    // ERE (elimination.cpp:169-197).
+    void ere() {
+        if (!opt.ere || !npvs) return;
+        if (opt.ere_max > 65535) throw std::runtime_error("eremax above 65535 is not supported");
+        EreArgs a;
+        a.c = view();
+        a.pvs = pvs.p;
+        a.npvs = npvs;
+        a.ere_max = (u32)opt.ere_max;
+        a.ere_clause_max = opt.ere_clause_max;
+        if (has_learnt) {
+            rt.one(FEreSeq{a});
+            rt.sync();
+            return;
+        }
+        ere_claim.reserve(rt, hdr.n);
+        rt.zero(ere_claim.p, (size_t)ncls * 8, 0xFF);
+        const size_t cap_rec = (size_t)ncls + (1u << 20);
+        ere_target.reserve(rt, cap_rec);
+        ere_key.reserve(rt, cap_rec);
+        ere_losers.reserve(rt, cap_rec);
+        a.claim = ere_claim.p;
+        a.rec_target = ere_target.p;
+        a.rec_key = ere_key.p;
+        a.nrec = counters.p + 7;
+        a.cap_rec = (u32)cap_rec;
+        a.losers = ere_losers.p;
+        a.nlosers = counters.p + 8;
+        write_u32(counters.p + 7, 0);
+        write_u32(counters.p + 8, 0);
+        rt.each(FEre{a}, npvs);
+        check();
+        const u32 nrec = read_u32(counters.p + 7);
+        rt.each(FEreResolve{a}, nrec);
+        const u32 nl = read_u32(counters.p + 8);
+        if (nl) {
+            std::vector<u32> L = fetch(ere_losers.p, nl);
+            std::vector<u64> K = fetch(ere_key.p, nrec);
+            std::vector<u64> keys(nl);
+            for (u32 i = 0; i < nl; i++) keys[i] = K[L[i]];
+            std::sort(keys.begin(), keys.end());
+            big64b.reserve(rt, nl + 1);
+            rt.h2d(big64b.p, keys.data(), nl * 8);
+            rt.one(FEreFix{a, big64b.p, nl});
+            rt.sync();
+        }
+    }
+
+    // countAll (solve.h:724-734).
+    void count_all() {
+        rt.zero(counters64.p + 2, 16);
+        CountArgs a{view(), counters64.p + 2};
+        rt.each(FCount{a}, ncls);
+        u64 h[2];
+        rt.d2h(h, counters64.p + 2, 16);
+        n_cls_after = (i64)h[0];
+        n_lits_after = (i64)h[1];
+    }
+
+    // shrinkSimp (simplify.cpp:234-245).
+    void gc() {
+        if (!ncls) return;
+        big32a.reserve(rt, (size_t)ncls + 1);
+        big32b.reserve(rt, (size_t)ncls + 1);
+        big64a.reserve(rt, (size_t)ncls + 1);
+        big64b.reserve(rt, (size_t)ncls + 1);
+        Ctx c = view();
+        rt.each(FGcFlags{c, big32a.p, big64a.p}, ncls);
+        const u32 keep = scan32(big32a.p, big32b.p, ncls);
+        const u64 keep_lits = scan64(big64a.p, big64b.p, ncls);
+        hdr2.reserve(rt, hdr.n);
+        lits2.reserve(rt, std::max<size_t>(lits.n, (size_t)keep_lits + 16));
+        GcArgs g{c, big32b.p, big64b.p, hdr2.p, lits2.p};
+        rt.each(FGcMove{g}, ncls);
+        std::swap(hdr, hdr2);
+        std::swap(lits, lits2);
+        alg_bytes += (4ull * nlits_used + 8ull * ncls) + (4ull * keep_lits + 8ull * keep);
+        ncls = keep;
+        nlits_used = keep_lits;
+    }
+
+    // resizeCNF (solve.h:684-688).
+    void resize_cnf() {
+        const int times = phase + 1;
+        if (opt.gc_freq > 0 && times > 1 && times != opt.phases && (times % opt.gc_freq) == 0) gc();
+    }
+
+    bool stop(i64 lr) const { return phase == opt.phases || (lr <= opt.ve_phase_min && phase > 2); }
+
+    double timed(int stage, void (pf_sigma_ctx::*fn)()) {
+        tm.start(rt);
+        (this->*fn)();
+        const double ms = tm.stop(rt);
+        st.ms_stage[stage] += ms;
+        return ms;
+    }
+
+    // sigmifying (simplify.cpp:182-209).
+    void round() {
+        phase = 0;
+        mu_inc = 0;
+        count_all();
+        i64 litsbefore = n_lits_after, diff = INT64_MAX;
+        st.clauses_before = (u64)n_cls_after;
+        st.literals_before = (u64)n_lits_after;
+        while (litsbefore) {
+            timed(ST_GC, &pf_sigma_ctx::resize_cnf);
+            timed(ST_OT, &pf_sigma_ctx::create_ot);
+            timed(ST_PROP, &pf_sigma_ctx::prop);
+            if (opt.dump_level >= 2) {
+                rec(2, phase, 1, fetch(ot_size.p, D));
+                dump_stage(phase, 1);
+            }
+            tm.start(rt);
+            const bool go = lcve();
+            st.ms_stage[ST_LCVE] += tm.stop(rt);
+            if (!go) break;
+            timed(ST_SORT, &pf_sigma_ctx::sort_ot);
+            if (opt.dump_level >= 2) dump_pvlists(phase);
+            const u64 W = pv_bytes();
+            alg_bytes += 2ull * W;  // sort reads and writes the lists (8*occ) ~ bounded by W
+            if (stop(diff)) {
+                timed(ST_ERE, &pf_sigma_ctx::ere);
+                alg_bytes += W;
+                dump_stage(phase, 7);
+                break;
+            }
+            timed(ST_SUB, &pf_sigma_ctx::sub);
+            dump_stage(phase, 4);
+            timed(ST_VE, &pf_sigma_ctx::ve);
+            dump_stage(phase, 5);
+            timed(ST_BCE, &pf_sigma_ctx::bce);
+            dump_stage(phase, 6);
+            alg_bytes += 4ull * W;
+            timed(ST_COUNT, &pf_sigma_ctx::count_all);
+            if (opt.dump_level >= 1) {
+                rec(10, phase, 6, {(u32)n_cls_after, (u32)n_lits_after});
+                dump_elim(phase, 6);
+            }
+            diff = litsbefore - n_lits_after;
+            litsbefore = n_lits_after;
+            phase++;
+            mu_inc++;
+            mu_inc += (phase == opt.phases);
+        }
+        timed(ST_PROP, &pf_sigma_ctx::prop);
+        timed(ST_COUNT, &pf_sigma_ctx::count_all);
+        timed(ST_GC, &pf_sigma_ctx::gc);
+        st.phases_run = phase;
+    }
+};
+
+// ---------------------------------------------------------------- C ABI
+static pf_status fail(const std::string& m, pf_status s) {
+    g_last_error = m;
+    return s;
+}
+
+template <class F>
+static pf_status guarded(F f) {
+    try {
+        return f();
+    } catch (int code) {
+        if (code == PF_UNSAT) return PF_UNSAT;
+        return fail("stopped with status " + std::to_string(code), (pf_status)code);
+    } catch (OomError& e) {
+        return fail(e.what(), PF_ENOMEM);
+    } catch (CudaError& e) {
+        return fail(e.what(), PF_EDEVICE);
+    } catch (std::exception& e) {
+        return fail(e.what(), PF_EDEVICE);
+    }
+}
+
+extern "C" {
+
+void pf_default_options(pf_options* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->phases = 5; o->all = 0; o->ve = 1; o->ve_plus = 1; o->sub = 1; o->bce = 0; o->ere = 1;
+    o->ve_lbound = 0; o->ve_clause_max = 100; o->ve_phase_min = 500; o->mu_pos = 32; o->mu_neg = 32;
+    o->xor_max_arity = 10; o->sub_max = 3000; o->bce_max = 3000; o->ere_max = 3000;
+    o->ere_clause_max = 1000; o->lcve_min = 1; o->gc_freq = 2; o->dump_level = 0;
+}
+
+void pf_derive_options(pf_options* o) {
+    o->ve = (o->ve || o->ve_plus) ? 1 : 0;
+    if (o->all) { o->ve = 1; o->ve_plus = 1; o->bce = 1; o->ere = 1; }
+    if (!o->phases && (o->ve || o->sub || o->bce)) o->phases = 1;
+    if (o->phases && !(o->ve || o->sub || o->bce)) o->phases = 0;
+    if (o->phases > 1 && !o->ve) o->phases = 1;
+}
+
+pf_status pf_sigma_create(const pf_options* opts, pf_sigma_ctx** out) {
+    if (!out) return fail("null output pointer", PF_EINVAL);
+    *out = nullptr;
+    pf_sigma_ctx* c = new pf_sigma_ctx();
+    try {
+        if (opts) c->opt = *opts;
+        else pf_default_options(&c->opt);
+        if (c->opt.xor_max_arity > 20 || c->opt.xor_max_arity < 2) {
+            delete c;
+            return fail("xormaxarity must be in [2, 20]", PF_EINVAL);
+        }
+        c->rt.init();
+        c->tm.init();
+        c->counters.reserve(c->rt, 32);
+        c->counters64.reserve(c->rt, 8);
+        c->rt.zero(c->counters.p, 32 * 4);
+        c->rt.zero(c->counters64.p, 8 * 8);
+        c->rt.sync();
+    } catch (std::exception& e) {
+        delete c;
+        return fail(e.what(), PF_EDEVICE);
+    }
+    *out = c;
+    return PF_OK;
+}
+
+static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint32_t* lits, const uint64_t* offsets,
+                               uint64_t num_clauses, const uint8_t* learnt, bool device) {
+    if (!ctx) return fail("null context", PF_EINVAL);
+    if (!lits || !offsets || num_vars == 0) return fail("null formula", PF_EINVAL);
+    if (num_vars >= (1u << 30)) return fail("too many variables", PF_EINVAL);
+    if (num_clauses >= 0xFFFFFF00ull) return fail("too many clauses", PF_EINVAL);
+    return guarded([&]() -> pf_status {
+        pf_sigma_ctx& c = *ctx;
+        Runtime& rt = c.rt;
+        u64 off0 = 0, offn = 0;
+        if (device) {
+            rt.d2h(&off0, offsets, 8);
+            rt.d2h(&offn, offsets + num_clauses, 8);
+        } else {
+            off0 = offsets[0];
+            offn = offsets[num_clauses];
+        }
+        if (offn < off0) return fail("offsets not ascending", PF_EINVAL);
+        const u64 L = offn - off0;
+        if (L >= 0xF0000000ull) return fail("too many literals", PF_EINVAL);
+        c.nvars = num_vars;
+        c.D = 2 * (num_vars + 1);
+        c.ncls = (u32)num_clauses;
+        c.nlits_used = L;
+        c.ntrail = c.prop_head = 0;
+        c.nresolved = 0;
+        c.has_learnt = false;
+        const size_t cap_cls = (size_t)num_clauses + num_clauses / 2 + 1024;
+        const size_t cap_lits = (size_t)L + L / 2 + 4096;
+        c.hdr.reserve(rt, cap_cls);
+        c.lits.reserve(rt, cap_lits);
+        c.cl_stamp.reserve(rt, cap_cls);
+        rt.zero(c.cl_stamp.p, cap_cls * 4);
+        c.wave_stamp = 0;
+        c.ot_off.reserve(rt, c.D + 1);
+        c.ot_size.reserve(rt, c.D);
+        c.ot_cursor.reserve(rt, c.D);
+        c.ot_refs.reserve(rt, cap_lits);
+        c.asg.reserve(rt, num_vars + 1);
+        c.vstate.reserve(rt, num_vars + 1);
+        c.ps.reserve(rt, num_vars + 1);
+        c.ns.reserve(rt, num_vars + 1);
+        c.pvrank.reserve(rt, num_vars + 1);
+        c.trail.reserve(rt, num_vars + 1);
+        c.resolved.reserve(rt, (size_t)L + 2 * (size_t)num_vars + 4096);
+        c.score.reserve(rt, num_vars + 1);
+        c.order.reserve(rt, num_vars + 1);
+        c.order_k2.reserve(rt, num_vars + 1);
+        c.order_v2.reserve(rt, num_vars + 1);
+        c.rank.reserve(rt, num_vars + 1);
+        c.bound.reserve(rt, 4);
+        c.pvs.reserve(rt, num_vars + 1);
+        c.flags.reserve(rt, num_vars + 1);
+        c.flags_scan.reserve(rt, num_vars + 1);
+        c.mis_state.reserve(rt, num_vars + 1);
+        c.radix_hist.reserve(rt, radix_hist_elems(num_vars + 1));
+        c.radix_hscan.reserve(rt, radix_hist_elems(num_vars + 1));
+        c.scan_tmp32.reserve(rt, scan_tmp_elems(std::max<size_t>(radix_hist_elems(num_vars + 1), cap_cls)) + 4);
+        rt.zero(c.asg.p, (size_t)(num_vars + 1) * 4);
+        rt.zero(c.vstate.p, num_vars + 1);
+        rt.zero(c.counters.p, 32 * 4);
+        rt.zero(c.counters64.p, 8 * 8);
+        // literals and offsets
+        DBuf<u64> doff;
+        DBuf<uint8_t> dlearnt;
+        const u64* off_ptr = offsets;
+        const uint8_t* learnt_ptr = learnt;
+        if (device) {
+            rt.d2d(c.lits.p, lits + off0, L * 4);
+        } else {
+            doff.reserve(rt, num_clauses + 1);
+            rt.h2d(c.lits.p, lits + off0, L * 4);
+            rt.h2d(doff.p, offsets, (num_clauses + 1) * 8);
+            off_ptr = doff.p;
+            if (learnt) {
+                dlearnt.reserve(rt, num_clauses + 1);
+                rt.h2d(dlearnt.p, learnt, num_clauses);
+                learnt_ptr = dlearnt.p;
+            }
+        }
+        if (learnt) {
+            std::vector<uint8_t> h(num_clauses);
+            if (device) rt.d2h(h.data(), learnt, num_clauses);
+            else std::memcpy(h.data(), learnt, num_clauses);
+            for (u64 i = 0; i < num_clauses; i++) if (h[i]) { c.has_learnt = true; break; }
+        }
+        UploadArgs a{c.view(), off_ptr, learnt_ptr, off0};
+        rt.each(FUpload{a}, (u32)num_clauses);
+        rt.sync();
+        doff.free();
+        dlearnt.free();
+        const u32 e = c.read_err();
+        if (e & ERR_INPUT) {
+            c.uploaded = false;
+            return fail("invalid clause (empty, literal out of range or repeated variable)", PF_EINVAL);
+        }
+        c.uploaded = true;
+        return PF_OK;
+    });
+}
+
+pf_status pf_sigma_upload(pf_sigma_ctx* ctx, uint32_t num_vars, const uint32_t* lits, const uint64_t* offsets,
+                          uint64_t num_clauses, const uint8_t* learnt) {
+    return upload_common(ctx, num_vars, lits, offsets, num_clauses, learnt, false);
+}
+
+pf_status pf_sigma_upload_device(pf_sigma_ctx* ctx, uint32_t num_vars, const uint32_t* d_lits,
+                                 const uint64_t* d_offsets, uint64_t num_clauses, const uint8_t* d_learnt) {
+    return upload_common(ctx, num_vars, d_lits, d_offsets, num_clauses, d_learnt, true);
+}
+
+pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
+    if (!ctx) return fail("null context", PF_EINVAL);
+    if (!ctx->uploaded) return fail("round before upload", PF_ESTATE);
+    pf_sigma_ctx& c = *ctx;
+    std::memset(&c.st, 0, sizeof(c.st));
+    c.dump.clear();
+    c.alg_bytes = 0;
+    c.rt.launches = 0;
+    pf_status status = PF_OK;
+    try {
+        pf_options& o = c.opt;
+        if (c.opt.dump_level > 0) {
+            c.dump_cnf(0, 0);
+            c.dump_trail(0, 0);
+        }
+        StageTimer whole;
+        whole.init();
+        whole.start(c.rt);
+        if (!(!o.phases && !(o.all || o.ere))) c.round();
+        c.st.ms_total = whole.stop(c.rt);
+        whole.destroy();
+        if (c.opt.dump_level > 0) {
+            c.dump_cnf(c.phase, 8);
+            c.dump_trail(c.phase, 8);
+            c.dump_resolved(c.phase, 8);
+            c.dump_elim(c.phase, 8);
+            c.rec(10, c.phase, 8, {(u32)c.n_cls_after, (u32)c.n_lits_after});
+        }
+    } catch (int code) {
+        status = (pf_status)code;
+        if (code != PF_UNSAT) g_last_error = "round stopped with status " + std::to_string(code);
+    } catch (OomError& e) {
+        status = fail(e.what(), PF_ENOMEM);
+    } catch (std::exception& e) {
+        status = fail(e.what(), PF_EDEVICE);
+    }
+    if (c.opt.dump_level > 0) c.rec(11, 0, 8, {status == PF_OK ? 0u : (status == PF_UNSAT ? 1u : 3u)});
+    c.st.status = status;
+    c.st.clauses_after = (u64)c.n_cls_after;
+    c.st.literals_after = (u64)c.n_lits_after;
+    c.st.units = c.ntrail;
+    c.st.resolved_words = c.nresolved;
+    c.st.algorithmic_bytes = c.alg_bytes;
+    c.st.kernel_launches = c.rt.launches;
+    if (stats) *stats = c.st;
+    return status;
+}
+
+pf_status pf_sigma_result_sizes(pf_sigma_ctx* ctx, uint64_t* num_clauses, uint64_t* num_literals, uint64_t* num_units,
+                                uint64_t* num_resolved) {
+    if (!ctx || !ctx->uploaded) return fail("no formula", PF_ESTATE);
+    if (num_clauses) *num_clauses = ctx->ncls;
+    if (num_literals) *num_literals = ctx->nlits_used;
+    if (num_units) *num_units = ctx->ntrail;
+    if (num_resolved) *num_resolved = ctx->nresolved;
+    return PF_OK;
+}
+
+pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets, uint8_t* learnt, uint32_t* units,
+                            uint32_t* resolved, uint8_t* eliminated) {
+    if (!ctx || !ctx->uploaded) return fail("no formula", PF_ESTATE);
+    return guarded([&]() -> pf_status {
+        pf_sigma_ctx& c = *ctx;
+        if (lits || offsets || learnt) {
+            auto H = c.fetch(c.hdr.p, c.ncls);
+            std::vector<u32> L;
+            if (lits) L = c.fetch(c.lits.p, c.nlits_used);
+            u64 o = 0;
+            for (u32 i = 0; i < c.ncls; i++) {
+                if (offsets) offsets[i] = o;
+                if (learnt) learnt[i] = h_learnt(H[i].flags) ? 1 : 0;
+                if (lits) std::memcpy(lits + o, L.data() + H[i].start, H[i].size * 4);
+                o += H[i].size;
+            }
+            if (offsets) offsets[c.ncls] = o;
+        }
+        if (units && c.ntrail) c.rt.d2h(units, c.trail.p, (size_t)c.ntrail * 4);
+        if (resolved && c.nresolved) c.rt.d2h(resolved, c.resolved.p, (size_t)c.nresolved * 4);
+        if (eliminated) c.rt.d2h(eliminated, c.vstate.p, c.nvars + 1);
+        return PF_OK;
+    });
+}
+
+pf_status pf_sigma_write_dump(pf_sigma_ctx* ctx, const char* path) {
+    if (!ctx || !path) return fail("null argument", PF_EINVAL);
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(std::string("cannot open ") + path, PF_EINVAL);
+    if (!ctx->dump.empty()) std::fwrite(ctx->dump.data(), 4, ctx->dump.size(), f);
+    std::fclose(f);
+    return PF_OK;
+}
+
+pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes) {
+    if (!ctx || !bytes) return fail("null argument", PF_EINVAL);
+    *bytes = ctx->rt.bytes_live;
+    return PF_OK;
+}
+
+void pf_sigma_destroy(pf_sigma_ctx* ctx) {
+    if (!ctx) return;
+    // DBuf members release themselves through the runtime
+    pf_sigma_ctx& c = *ctx;
+    DBuf<Hdr>* hb[] = {&c.hdr, &c.hdr2, &c.sub_hdrs};
+    for (auto* b : hb) b->free();
+    DBuf<u32>* b32[] = {&c.lits, &c.lits2, &c.ot_off, &c.ot_size, &c.ot_refs, &c.ot_cursor, &c.asg, &c.ps, &c.ns,
+                        &c.pvrank, &c.trail, &c.resolved, &c.counters, &c.score, &c.order, &c.order_k2,
+                        &c.order_v2, &c.rank, &c.bound, &c.pvs, &c.flags, &c.flags_scan, &c.work, &c.cl_stamp,
+                        &c.radix_hist, &c.radix_hscan, &c.scan_tmp32, &c.big32a, &c.big32b, &c.ve_porgs,
+                        &c.ve_norgs, &c.ve_ncls, &c.ve_nlits, &c.ve_nwit, &c.ve_def, &c.ve_cls_scan, &c.ve_scr,
+                        &c.sub_ent, &c.sub_ent_off, &c.sub_ids, &c.sub_words, &c.sub_sizes, &c.sub_pre_off,
+                        &c.sub_pre_lits, &c.sub_ulits, &c.ere_target, &c.ere_losers};
+    for (auto* b : b32) b->free();
+    DBuf<u64>* b64[] = {&c.counters64, &c.scan_tmp64, &c.big64a, &c.big64b, &c.ve_scr_off, &c.ve_lit_scan,
+                        &c.ve_wit_scan, &c.sub_wrd, &c.sub_wrd_off, &c.ere_claim, &c.ere_key};
+    for (auto* b : b64) b->free();
+    DBuf<uint8_t>* b8[] = {&c.vstate, &c.mis_state, &c.ve_type, &c.sub_run};
+    for (auto* b : b8) b->free();
+    c.sub_units.free();
+    c.sub_pairs.free();
+    c.tm.destroy();
+    c.rt.destroy();
+    delete ctx;
+}
+
+const char* pf_last_error(void) { return g_last_error.c_str(); }
+
+}  // extern "C"

@@ -58,6 +58,43 @@ def canonical(recs: list) -> dict:
     return res
 
 
+def normalize(recs: list) -> list:
+    """Mask what parallel unit propagation may legitimately change.
+
+    The reference strips false literals one trail literal at a time, so a clause
+    that ends up deleted keeps whichever false literals it still had when a true
+    literal reached it; the GPU's wave-parallel propagation can strip a different
+    subset. Live clauses, statuses, units and every later decision are the same.
+    Deleted clauses therefore compare by status only, and sorted occurrence lists
+    compare without their deleted entries (whose position follows their content).
+    """
+    out, deleted = [], {}
+    for kind, phase, stage, d in recs:
+        if kind == "cnf":
+            cl = cnf_clauses(d)
+            flat = [len(cl)]
+            dele = set()
+            for i, (f, sig, lits) in enumerate(cl):
+                if (f & 3) == 2:
+                    flat += [2, 0, 0]
+                    dele.add(i)
+                else:
+                    flat += [f, sig, len(lits)] + list(lits)
+            deleted[(phase, stage)] = dele
+            d = np.array(flat, dtype=np.uint32)
+        elif kind == "pvlists":
+            dele = deleted.get((phase, "prop"), set())
+            flat, i = [], 0
+            while i < d.size:
+                n = int(d[i])
+                keep = [int(x) for x in d[i + 1:i + 1 + n] if int(x) not in dele]
+                flat += [len(keep)] + keep
+                i += 1 + n
+            d = np.array(flat, dtype=np.uint32)
+        out.append((kind, phase, stage, d))
+    return out
+
+
 def _key(rec):
     kind, phase, stage, _ = rec
     return (kind, phase, stage)

@@ -1,0 +1,190 @@
+"""Python binding of libsigma_gb300.so (the ctypes form of the C ABI in
+include/sigma_gb300.h).
+
+``Simplifier`` mirrors the reference's simplifier entry points: construct it
+with the reference option names (``Options``), ``awaken()`` uploads a formula
+(ParaFROST::awaken/extract, src/cpu/simplify.cpp:95-155), ``sigmify()`` runs one
+round (ParaFROST::sigmify, simplify.cpp:115-129) and ``result()`` returns the
+simplified formula, units, witness stack and eliminated flags. Errors raise
+``SigmaError`` with the library's status; a proved contradiction is reported as
+``status == PF_UNSAT`` (the reference's learnEmpty + killSolver path).
+
+The product path loads the CUDA library only and raises when it is missing or
+no GPU is visible; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from .options import Options, PfOptions
+
+PF_OK, PF_UNSAT, PF_EINVAL, PF_ENOMEM, PF_ETIMEOUT, PF_EDEVICE, PF_ESTATE = 0, 1, -1, -2, -3, -4, -5
+STATUS_NAMES = {0: "PF_OK", 1: "PF_UNSAT", -1: "PF_EINVAL", -2: "PF_ENOMEM", -3: "PF_ETIMEOUT",
+                -4: "PF_EDEVICE", -5: "PF_ESTATE"}
+STAGES = ["ot", "prop", "lcve", "sort", "sub", "ve", "bce", "ere", "gc", "count", "upload", "download"]
+
+
+class SigmaError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class RoundStats(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("phases_run", ctypes.c_int32),
+                ("clauses_before", ctypes.c_uint64), ("literals_before", ctypes.c_uint64),
+                ("clauses_after", ctypes.c_uint64), ("literals_after", ctypes.c_uint64),
+                ("eliminated_vars", ctypes.c_uint64), ("units", ctypes.c_uint64),
+                ("resolved_words", ctypes.c_uint64), ("ms_total", ctypes.c_double),
+                ("ms_stage", ctypes.c_double * 12), ("algorithmic_bytes", ctypes.c_uint64),
+                ("kernel_launches", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 3)]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("ms_stage", "reserved")}
+        d["ms_stage"] = {s: self.ms_stage[i] for i, s in enumerate(STAGES)}
+        return d
+
+
+_VP, _U32, _U64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64
+
+
+def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
+    lib.pf_default_options.argtypes = [_VP]
+    lib.pf_derive_options.argtypes = [_VP]
+    lib.pf_sigma_create.argtypes = [_VP, ctypes.POINTER(_VP)]
+    lib.pf_sigma_create.restype = ctypes.c_int
+    lib.pf_sigma_upload.argtypes = [_VP, _U32, _VP, _VP, _U64, _VP]
+    lib.pf_sigma_upload.restype = ctypes.c_int
+    lib.pf_sigma_upload_device.argtypes = [_VP, _U32, _VP, _VP, _U64, _VP]
+    lib.pf_sigma_upload_device.restype = ctypes.c_int
+    lib.pf_sigma_round.argtypes = [_VP, _VP]
+    lib.pf_sigma_round.restype = ctypes.c_int
+    lib.pf_sigma_result_sizes.argtypes = [_VP, _VP, _VP, _VP, _VP]
+    lib.pf_sigma_result_sizes.restype = ctypes.c_int
+    lib.pf_sigma_download.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
+    lib.pf_sigma_download.restype = ctypes.c_int
+    lib.pf_sigma_write_dump.argtypes = [_VP, ctypes.c_char_p]
+    lib.pf_sigma_write_dump.restype = ctypes.c_int
+    lib.pf_sigma_footprint.argtypes = [_VP, _VP]
+    lib.pf_sigma_footprint.restype = ctypes.c_int
+    lib.pf_sigma_destroy.argtypes = [_VP]
+    lib.pf_sigma_destroy.restype = None
+    lib.pf_last_error.argtypes = []
+    lib.pf_last_error.restype = ctypes.c_char_p
+    return lib
+
+
+_LIBS: dict = {}
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Load the CUDA library (default) or an explicit library path."""
+    from . import build
+    path = path or build.LIB
+    if path not in _LIBS:
+        if not os.path.exists(path):
+            raise SigmaError(PF_EDEVICE, f"CUDA library not built: {path} (run __graft_entry__.build())")
+        _LIBS[path] = _bind(ctypes.CDLL(path))
+    return _LIBS[path]
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+@dataclass
+class Result:
+    num_vars: int
+    lits: np.ndarray       # uint32, clause literals in clause-store order
+    offsets: np.ndarray    # uint64, num_clauses + 1
+    learnt: np.ndarray     # uint8 per clause
+    units: np.ndarray      # uint32, assigned literals
+    resolved: np.ndarray   # uint32, witness stack (model.resolved)
+    eliminated: np.ndarray # uint8 per variable (index 0 unused)
+
+    def clauses(self) -> list:
+        o = self.offsets.astype(np.int64)
+        return [tuple(int(x) for x in self.lits[o[i]:o[i + 1]]) for i in range(o.size - 1)]
+
+
+class Simplifier:
+    """One resident formula on the current GPU (a pf_sigma_ctx)."""
+
+    def __init__(self, opts: Options | None = None, library: str | None = None):
+        self.lib = load_library(library)
+        self.opts = (opts or Options()).derived()
+        self._o = self.opts.to_struct()
+        h = _VP()
+        st = self.lib.pf_sigma_create(ctypes.addressof(self._o), ctypes.byref(h))
+        self._check(st)
+        self.h = h
+        self.num_vars = 0
+
+    def _check(self, st: int) -> int:
+        if st not in (PF_OK, PF_UNSAT):
+            raise SigmaError(st, self.lib.pf_last_error().decode(errors="replace"))
+        return st
+
+    def awaken(self, num_vars: int, lits: np.ndarray, offsets: np.ndarray, learnt: np.ndarray | None = None) -> None:
+        """Upload a formula from host arrays (ParaFROST::awaken/extract)."""
+        lits = np.ascontiguousarray(lits, dtype=np.uint32)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        if learnt is not None:
+            learnt = np.ascontiguousarray(learnt, dtype=np.uint8)
+        self._check(self.lib.pf_sigma_upload(self.h, num_vars, _ptr(lits), _ptr(offsets), offsets.size - 1,
+                                             _ptr(learnt)))
+        self.num_vars = num_vars
+
+    def awaken_device(self, num_vars: int, d_lits: int, d_offsets: int, num_clauses: int, d_learnt: int | None = None):
+        """Upload from device pointers (e.g. torch tensors' data_ptr())."""
+        self._check(self.lib.pf_sigma_upload_device(self.h, num_vars, d_lits, d_offsets, num_clauses, d_learnt))
+        self.num_vars = num_vars
+
+    def sigmify(self) -> RoundStats:
+        """One sigmify round. stats.status is PF_OK or PF_UNSAT."""
+        stats = RoundStats()
+        self._check(self.lib.pf_sigma_round(self.h, ctypes.byref(stats)))
+        return stats
+
+    def result(self) -> Result:
+        nc, nl, nu, nr = _U64(), _U64(), _U64(), _U64()
+        self._check(self.lib.pf_sigma_result_sizes(self.h, ctypes.byref(nc), ctypes.byref(nl), ctypes.byref(nu),
+                                                   ctypes.byref(nr)))
+        lits = np.empty(nl.value, dtype=np.uint32)
+        offsets = np.empty(nc.value + 1, dtype=np.uint64)
+        learnt = np.empty(nc.value, dtype=np.uint8)
+        units = np.empty(nu.value, dtype=np.uint32)
+        resolved = np.empty(nr.value, dtype=np.uint32)
+        elim = np.empty(self.num_vars + 1, dtype=np.uint8)
+        self._check(self.lib.pf_sigma_download(self.h, _ptr(lits), _ptr(offsets), _ptr(learnt), _ptr(units),
+                                               _ptr(resolved), _ptr(elim)))
+        return Result(self.num_vars, lits, offsets, learnt, units, resolved, elim)
+
+    def write_dump(self, path: str) -> None:
+        self._check(self.lib.pf_sigma_write_dump(self.h, path.encode()))
+
+    def footprint(self) -> int:
+        b = _U64()
+        self._check(self.lib.pf_sigma_footprint(self.h, ctypes.byref(b)))
+        return b.value
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.pf_sigma_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
