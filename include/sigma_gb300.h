@@ -124,6 +124,18 @@ pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets
 /* Writes the per-stage round dump of the last round to path (dump_level > 0). */
 pf_status pf_sigma_write_dump(pf_sigma_ctx* ctx, const char* path);
 
+/* Builds the occurrence table of a clause list (createOTAsync, src/gpu/kernels.cu:949-982
+ * with resizeOTAsync's scan, memory.cu:271-312; CPU createOT, simplify.cpp:35-56).
+ * All pointers are device memory: clause c has literals d_lits[d_offsets[c] ..
+ * d_offsets[c+1]) (offsets relative to d_lits), literals in [2, 2*num_vars+2).
+ * Outputs: d_ot_off[2*num_vars+3] (list starts, last = total), d_ot_size[2*num_vars+2]
+ * (list sizes), d_ot_refs[total literals] (clause indices; order inside a list is
+ * unspecified). stream is a cudaStream_t (NULL = legacy default stream). The scan
+ * scratch is allocated and freed inside the call; the call returns after the
+ * stream has finished. */
+pf_status pf_create_ot(uint32_t num_vars, const uint32_t* d_lits, const uint64_t* d_offsets, uint64_t num_clauses,
+                       uint32_t* d_ot_off, uint32_t* d_ot_size, uint32_t* d_ot_refs, void* stream);
+
 /* Device bytes held by the context. */
 pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes);
 

@@ -62,6 +62,37 @@ HD void k_scatter_clause(const Ctx& c, u32 i) {
     }
 }
 
+// Standalone occurrence-table build over a clause list in CSR form (all clauses
+// live): histogram into ot_size, exclusive scan into ot_off, then a scatter that
+// reuses ot_size (zeroed after the scan) as the per-literal cursor, which leaves
+// the list sizes in ot_size again.
+struct CsrOtArgs {
+    const u32* lits;
+    const u64* off;
+    u32* ot_off;
+    u32* ot_size;
+    u32* ot_refs;
+    u64 nlits;
+    u32 D;
+    u32* err;
+};
+HD void k_hist_csr(const CsrOtArgs& a, u32 i) {
+    for (u64 k = a.off[i]; k < a.off[i + 1]; k++) {
+        const u32 lit = a.lits[k];
+        if (lit < 2 || lit >= a.D) { atom_or(a.err, ERR_INPUT); continue; }
+        atom_add(&a.ot_size[lit], 1u);
+    }
+}
+HD void k_scatter_csr(const CsrOtArgs& a, u32 i) {
+    for (u64 k = a.off[i]; k < a.off[i + 1]; k++) {
+        const u32 lit = a.lits[k];
+        if (lit < 2 || lit >= a.D) continue;
+        const u32 pos = a.ot_off[lit] + atom_add(&a.ot_size[lit], 1u);
+        if (pos < a.nlits) a.ot_refs[pos] = i;
+        else atom_or(a.err, ERR_INTERNAL);
+    }
+}
+
 // occurs[v] = (ps, ns) over live clauses (histSimp, src/cpu/histogram.cpp:82-96).
 HD void k_occurs_clause(const Ctx& c, u32 i) {
     const Hdr h = c.hdr[i];

@@ -1040,6 +1040,59 @@ pf_status pf_sigma_write_dump(pf_sigma_ctx* ctx, const char* path) {
     return PF_OK;
 }
 
+struct FHistCsr { CsrOtArgs a; HD void operator()(u32 i) const { k_hist_csr(a, i); } };
+struct FScatterCsr { CsrOtArgs a; HD void operator()(u32 i) const { k_scatter_csr(a, i); } };
+
+// Histogram -> scan -> scatter over caller buffers; `tmp` holds the scan block sums
+// (scan_tmp_elems(D) words) followed by one error word.
+static void create_ot_into(Runtime& rt, u32 num_vars, const u32* d_lits, const u64* d_offsets, u64 num_clauses,
+                           u32* d_ot_off, u32* d_ot_size, u32* d_ot_refs, u32* tmp, size_t tmp_words) {
+    const u32 D = 2 * (num_vars + 1);
+    u32* err = tmp + tmp_words - 1;
+    u64 off0 = 0, offn = 0;
+    rt.d2h(&off0, d_offsets, 8);
+    rt.d2h(&offn, d_offsets + num_clauses, 8);
+    CsrOtArgs a{d_lits, d_offsets, d_ot_off, d_ot_size, d_ot_refs, offn - off0, D, err};
+    if (off0 != 0) throw int(PF_EINVAL);
+    rt.zero(err, 4);
+    rt.zero(d_ot_size, (size_t)D * 4);
+    rt.each(FHistCsr{a}, (u32)num_clauses);
+    excl_scan<u32, u32>(d_ot_size, d_ot_off, D, d_ot_off + D, tmp, rt.stream);
+    rt.zero(d_ot_size, (size_t)D * 4);
+    rt.each(FScatterCsr{a}, (u32)num_clauses);
+    u32 e = 0;
+    rt.d2h(&e, err, 4);
+    if (e & ERR_INPUT) throw int(PF_EINVAL);
+    if (e) throw std::runtime_error("occurrence table build failed");
+}
+
+pf_status pf_create_ot(uint32_t num_vars, const uint32_t* d_lits, const uint64_t* d_offsets, uint64_t num_clauses,
+                       uint32_t* d_ot_off, uint32_t* d_ot_size, uint32_t* d_ot_refs, void* stream) {
+    if (!d_lits || !d_offsets || !d_ot_off || !d_ot_size || !d_ot_refs || !num_vars) return fail("null argument", PF_EINVAL);
+    if (num_vars >= (1u << 30) || num_clauses >= 0xFFFFFF00ull) return fail("formula too large", PF_EINVAL);
+    Runtime rt;
+    return guarded([&]() -> pf_status {
+        rt.init();
+#if SIGMA_CUDA
+        cudaStreamDestroy(rt.stream);
+        rt.stream = (cudaStream_t)stream;
+#endif
+        const u32 D = 2 * (num_vars + 1);
+        const size_t words = scan_tmp_elems(D) + 1;
+        u32* tmp = (u32*)rt.alloc(words * 4);
+        try {
+            create_ot_into(rt, num_vars, d_lits, d_offsets, num_clauses, d_ot_off, d_ot_size, d_ot_refs, tmp, words);
+        } catch (...) {
+            rt.sync();
+            rt.release(tmp, words * 4);
+            throw;
+        }
+        rt.sync();
+        rt.release(tmp, words * 4);
+        return PF_OK;
+    });
+}
+
 pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes) {
     if (!ctx || !bytes) return fail("null argument", PF_EINVAL);
     *bytes = ctx->rt.bytes_live;

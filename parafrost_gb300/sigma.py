@@ -73,6 +73,8 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     lib.pf_sigma_footprint.restype = ctypes.c_int
     lib.pf_sigma_destroy.argtypes = [_VP]
     lib.pf_sigma_destroy.restype = None
+    lib.pf_create_ot.argtypes = [_U32, _VP, _VP, _U64, _VP, _VP, _VP, _VP]
+    lib.pf_create_ot.restype = ctypes.c_int
     lib.pf_last_error.argtypes = []
     lib.pf_last_error.restype = ctypes.c_char_p
     return lib
@@ -94,6 +96,25 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
 
 def _ptr(a: np.ndarray | None):
     return None if a is None else a.ctypes.data
+
+
+def create_ot(num_vars: int, d_lits: int, d_offsets: int, num_clauses: int, d_ot_off: int, d_ot_size: int,
+              d_ot_refs: int, stream: int | None = None, library: str | None = None) -> None:
+    """Occurrence table of a clause list held in device memory (pf_create_ot)."""
+    lib = load_library(library)
+    st = lib.pf_create_ot(num_vars, d_lits, d_offsets, num_clauses, d_ot_off, d_ot_size, d_ot_refs, stream)
+    if st != PF_OK:
+        raise SigmaError(st, lib.pf_last_error().decode(errors="replace"))
+
+
+def occurrence_lists(num_vars: int, lits: np.ndarray, offsets: np.ndarray):
+    """Host restatement of the table's content: per literal, the sorted clause indices."""
+    owner = np.repeat(np.arange(offsets.size - 1, dtype=np.uint32), np.diff(offsets.astype(np.int64)))
+    order = np.lexsort((owner, lits))
+    D = 2 * (num_vars + 1)
+    size = np.bincount(lits, minlength=D).astype(np.uint32)
+    off = np.concatenate([[0], np.cumsum(size)]).astype(np.uint32)
+    return off, size, owner[order]
 
 
 @dataclass
