@@ -136,6 +136,25 @@ pf_status pf_sigma_write_dump(pf_sigma_ctx* ctx, const char* path);
 pf_status pf_create_ot(uint32_t num_vars, const uint32_t* d_lits, const uint64_t* d_offsets, uint64_t num_clauses,
                        uint32_t* d_ot_off, uint32_t* d_ot_size, uint32_t* d_ot_refs, void* stream);
 
+/* pf_create_ot without any allocation. No counterpart in the reference.
+ *
+ * For callers that must not allocate device memory: a serving process whose HBM
+ * is fully reserved up front by its own pool or by a framework's caching
+ * allocator (where a cudaMalloc can fail or escape the budget), or a caller that
+ * cannot take the device-wide synchronisation a cudaFree implies. Inputs and
+ * outputs are the caller's device buffers, exactly as for pf_create_ot; the scan
+ * scratch lives in a fixed 256 KiB array inside the library (held by every GPU
+ * that loads the library until the process exits). Limit: num_vars <= 67,100,000
+ * (2*num_vars+2 literal slots in 65,534 scan blocks of 2048); larger formulas get
+ * PF_EINVAL. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture. All calls share the one array: calls that overlap on the
+ * GPU (other streams, other threads) race; serialise them. Calls no cudaMalloc,
+ * cudaFree or other allocating routine, and creates no stream. */
+pf_status pf_create_ot_noalloc(uint32_t num_vars, const uint32_t* d_lits, const uint64_t* d_offsets,
+                               uint64_t num_clauses, uint32_t* d_ot_off, uint32_t* d_ot_size, uint32_t* d_ot_refs,
+                               void* stream);
+
 /* Device bytes held by the context. */
 pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes);
 

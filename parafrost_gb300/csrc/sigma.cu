@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <climits>
 #include <map>
+#include <mutex>
 #include <set>
 #include <vector>
 
@@ -1089,6 +1090,61 @@ pf_status pf_create_ot(uint32_t num_vars, const uint32_t* d_lits, const uint64_t
         }
         rt.sync();
         rt.release(tmp, words * 4);
+        return PF_OK;
+    });
+}
+
+// ---------------------------------------------------------------- no-allocation variant
+// pf_create_ot_noalloc: the scan scratch (block sums + one error word) is this
+// fixed array instead of a cudaMalloc. In host code its name only stands in for
+// the device symbol; the device address comes from cudaGetSymbolAddress, looked
+// up once per device on that device's first call.
+constexpr u32 kNoallocWords = 1u << 16;  // 256 KiB
+#if SIGMA_CUDA
+static __device__ __align__(256) u32 g_noalloc_scratch[kNoallocWords];
+#else
+alignas(256) static u32 g_noalloc_scratch[kNoallocWords];
+#endif
+static std::mutex g_noalloc_mu;
+static u32* g_noalloc_dev[256];  // per device ordinal
+
+static u32* noalloc_scratch_ptr() {
+#if SIGMA_CUDA
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 256) throw std::runtime_error("device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_dev[dev]) {
+        void* p = nullptr;
+        ck(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress");
+        g_noalloc_dev[dev] = (u32*)p;
+    }
+    return g_noalloc_dev[dev];
+#else
+    return g_noalloc_scratch;
+#endif
+}
+
+pf_status pf_create_ot_noalloc(uint32_t num_vars, const uint32_t* d_lits, const uint64_t* d_offsets,
+                               uint64_t num_clauses, uint32_t* d_ot_off, uint32_t* d_ot_size, uint32_t* d_ot_refs,
+                               void* stream) {
+    if (!d_lits || !d_offsets || !d_ot_off || !d_ot_size || !d_ot_refs || !num_vars) return fail("null argument", PF_EINVAL);
+    if (num_clauses >= 0xFFFFFF00ull) return fail("too many clauses", PF_EINVAL);
+    const u64 D = 2ull * ((u64)num_vars + 1);
+    if (num_vars >= (1u << 30) || scan_tmp_elems(D) + 1 > kNoallocWords)
+        return fail("pf_create_ot_noalloc: num_vars above 67,100,000 exceeds the fixed scratch", PF_EINVAL);
+    return guarded([&]() -> pf_status {
+        Runtime rt;  // no init(): this call creates no stream and allocates nothing
+#if SIGMA_CUDA
+        int dev = 0;
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        ck(cudaDeviceGetAttribute(&rt.sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+        rt.stream = (cudaStream_t)stream;
+#endif
+        u32* scratch = noalloc_scratch_ptr();
+        create_ot_into(rt, num_vars, d_lits, d_offsets, num_clauses, d_ot_off, d_ot_size, d_ot_refs, scratch,
+                       kNoallocWords);
+        rt.sync();
         return PF_OK;
     });
 }
