@@ -76,7 +76,8 @@ typedef struct {
     double ms_stage[12];      /* ot, prop, lcve, sort, sub, ve, bce, ere, gc, count, upload, download */
     uint64_t algorithmic_bytes; /* bytes the round's kernels must move (HBM roofline numerator) */
     uint32_t kernel_launches;   /* kernels launched by the round */
-    uint32_t reserved[3];
+    uint32_t mis_rounds;        /* parallel independent-set rounds of the elections */
+    uint32_t reserved[2];
 } pf_round_stats;
 
 typedef struct pf_sigma_ctx pf_sigma_ctx;

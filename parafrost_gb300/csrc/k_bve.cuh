@@ -245,8 +245,14 @@ HD bool find_ao_gate(const BveArgs& a, u32 dx, int nOrgCls, u32* out, int& nAdde
 
 // ---------------------------------------------------------------- ITE
 // fast_equality_check (ifthenelse.h:25-40): the original, unmolten ternary (x y z)
-// in the shortest of the three lists; NONE if absent.
+// in the shortest of the three lists; NONE if absent. The first argument is always
+// the elected variable's own literal, so every clause that can match is in that
+// literal's own list: the search scans the own list and returns the first match in
+// its order when the reference picks the own list, else the smallest matching id
+// (the reference's first match in a neighbour list, which it keeps in clause-store
+// order, among the same set of live matching clauses).
 HD u32 fast_equality_check(const Ctx& c, u32 v, u32 x, u32 y, u32 z) {
+    const u32 ownlit = x;
     if (c.ot_size[y] > c.ot_size[z]) swap_t(y, z);
     if (c.ot_size[x] > c.ot_size[y]) swap_t(x, y);
     const u32 ll = x;
@@ -254,8 +260,9 @@ HD u32 fast_equality_check(const Ctx& c, u32 v, u32 x, u32 y, u32 z) {
     { const u32 lo = y < z ? y : z, hi = y < z ? z : y; y = lo; z = hi; }
     { const u32 lo = x < z ? x : z, hi = x < z ? z : x; x = lo; z = hi; }
     { const u32 lo = x < y ? x : y, hi = x < y ? y : x; x = lo; y = hi; }
-    const ListRef L = list_of(c, ll);
-    const bool own = ABS(ll) == v;
+    const ListRef L = list_of(c, ownlit);
+    const bool own = ll == ownlit;
+    (void)v;
     u32 best = NONE;
     for (u32 i = 0; i < L.n; i++) {
         const u32 r = L.ids[i];
@@ -337,12 +344,16 @@ HD bool make_arity(const Ctx& c, u32 v, u32& parity, u32* lits, int size) {
     }
     u32 best = lits[0];
     u32 minsize = c.ot_size[best];
+    u32 ownlit = lits[0];
     for (int k = 1; k < size; k++) {
         const u32 ls = c.ot_size[lits[k]];
         if (ls < minsize) { minsize = ls; best = lits[k]; }
     }
-    const ListRef L = list_of(c, best);
-    const bool own = ABS(best) == v;
+    for (int k = 0; k < size; k++) if (ABS(lits[k]) == v) ownlit = lits[k];
+    // Every clause that can match holds the variable's own literal: scan that list
+    // (see fast_equality_check for why the result is the reference's).
+    const ListRef L = list_of(c, ownlit);
+    const bool own = best == ownlit;
     u32 found = NONE;
     for (u32 i = 0; i < L.n; i++) {
         const u32 r = L.ids[i];

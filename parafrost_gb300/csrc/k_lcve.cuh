@@ -55,39 +55,66 @@ HD void k_rank(const LcveArgs& a, u32 p) {
     if (lcve_valid(a.c, v) && !lcve_freezable(a, v)) atom_min(&a.bound[0], p);
 }
 
-HD void k_mis_init(const LcveArgs& a, u32 v) {
+// Work lists of undecided vertices and, per vertex, where its last scan met the first
+// undecided lower neighbour (side:1 | list index:23 | literal index:8). Everything
+// before that point was out or irrelevant, and "out" is final, so the next round
+// resumes there. Indices are capped, which only makes a scan start earlier.
+struct MisList {
+    u32* resume;
+    const u32* in;
+    u32* out;
+    u32* nout;
+};
+
+HD u32 mis_pos(u32 side, u32 i, u32 k) {
+    if (i >= 0x7FFFFFu) return (side << 31) | (0x7FFFFFu << 8);  // restart that clause from its first literal
+    return (side << 31) | (i << 8) | (k < 255u ? k : 255u);
+}
+
+HD void k_mis_init(const LcveArgs& a, const MisList& w, u32 v) {
     if (v == 0) { a.state[0] = MIS_NONE; return; }
     const bool in_graph = lcve_valid(a.c, v) && lcve_freezable(a, v) && a.rank[v] < a.bound[0];
     a.state[v] = in_graph ? MIS_UNDECIDED : MIS_NONE;
+    if (in_graph) {
+        w.resume[v] = 0;
+        w.out[atom_add(w.nout, 1u)] = v;
+    }
 }
 
-// One round for an undecided vertex v: scan its live clauses.
-HD void k_mis_round(const LcveArgs& a, u32 v) {
-    if (v == 0) return;
+// One round for an undecided vertex: scan its live clauses from the resume point.
+HD void k_mis_round(const LcveArgs& a, const MisList& w, u32 idx) {
+    const u32 v = w.in[idx];
     volatile uint8_t* st = (volatile uint8_t*)a.state;
     if (st[v] != MIS_UNDECIDED) return;
     const Ctx& c = a.c;
     const u32 rv = a.rank[v];
-    bool pending = false;
-    for (u32 side = 0; side < 2; side++) {
+    const u32 pos = w.resume[v];
+    const u32 side0 = pos >> 31, i0 = (pos >> 8) & 0x7FFFFFu, k0 = pos & 0xFFu;
+    u32 first = NONE;
+    for (u32 side = side0; side < 2; side++) {
         const u32 l = V2L(v) + side;
         const u32 o = c.ot_off[l], s = c.ot_size[l];
-        for (u32 i = 0; i < s; i++) {
+        for (u32 i = side == side0 ? i0 : 0u; i < s; i++) {
             const Hdr h = c.hdr[c.ot_refs[o + i]];
             if (h_deleted(h.flags)) continue;
             const u32* lits = c.lits + h.start;
-            for (u32 k = 0; k < h.size; k++) {
+            const u32 kstart = (side == side0 && i == i0) ? k0 : 0u;
+            for (u32 k = kstart; k < h.size; k++) {
                 const u32 u = ABS(lits[k]);
                 if (u == v) continue;
                 const uint8_t su = st[u];
                 if (su == MIS_NONE || a.rank[u] > rv) continue;
                 if (su == MIS_IN) { st[v] = MIS_OUT; return; }
-                if (su == MIS_UNDECIDED) pending = true;
+                if (su == MIS_UNDECIDED && first == NONE) first = mis_pos(side, i, k);
             }
         }
     }
-    if (!pending) st[v] = MIS_IN;
-    else atom_add(a.changed, 1u);
+    if (first == NONE) {
+        st[v] = MIS_IN;
+    } else {
+        w.resume[v] = first;
+        w.out[atom_add(w.nout, 1u)] = v;
+    }
 }
 
 // B = min(B0, first member whose lists reach the temperatures).

@@ -32,14 +32,18 @@ struct IdLess {
 struct SortArgs {
     Ctx c;
     const u32* pvs;
+    u64* ws_bytes;  // accumulates the elected lists' working set (4*occ + sum(8 + 4*len))
 };
 
 // One item per list: 2*k is the positive list of pvs[k], 2*k+1 the negative one.
 HD void k_sort_list(const SortArgs& a, u32 k) {
     const u32 l = V2L(a.pvs[k >> 1]) + (k & 1u);
     const u32 n = a.c.ot_size[l];
-    if (n <= 1) return;
     u32* d = a.c.ot_refs + a.c.ot_off[l];
+    u64 ws = 4ull * n;
+    for (u32 i = 0; i < n; i++) ws += 8ull + 4ull * a.c.hdr[d[i]].size;
+    atom_add64(a.ws_bytes, ws);
+    if (n <= 1) return;
     if (n <= 20) ref_insertion_sort(d, (int)n, IdLess());
     else std_sort_replica(d, d + n, IdLess());
     reference_list_sort(d, (int)n, KeyLess{a.c.hdr, a.c.lits});

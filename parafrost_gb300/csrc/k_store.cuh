@@ -125,6 +125,31 @@ HD void k_count_clause(const CountArgs& a, u32 i) {
     atom_add64(&a.out[1], (u64)h.size);
 }
 
+#if SIGMA_CUDA
+// Same counts with a warp/block reduction and one pair of atomics per block.
+__global__ void count_live_k(const Hdr* __restrict__ hdr, u32 n, u64* out) {
+    u64 cls = 0, lits = 0;
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += blockDim.x * gridDim.x) {
+        const Hdr h = hdr[i];
+        if (!h_deleted(h.flags)) { cls++; lits += h.size; }
+    }
+    for (int o = 16; o; o >>= 1) {
+        cls += __shfl_down_sync(0xffffffffu, cls, o);
+        lits += __shfl_down_sync(0xffffffffu, lits, o);
+    }
+    __shared__ u64 s_cls[32], s_lits[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { s_cls[warp] = cls; s_lits[warp] = lits; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        u64 c = 0, l = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { c += s_cls[w]; l += s_lits[w]; }
+        atomicAdd((unsigned long long*)&out[0], (unsigned long long)c);
+        atomicAdd((unsigned long long*)&out[1], (unsigned long long)l);
+    }
+}
+#endif
+
 // ---------------------------------------------------------------- compaction
 // shrinkSimp (src/cpu/simplify.cpp:234-245; GPU: recycle.cu:30-97): drop deleted
 // clauses, keep order. Two exclusive scans (kept clauses, kept literals) give the

@@ -42,8 +42,8 @@ struct FPropClause { PropArgs a; HD void operator()(u32 i) const { k_prop_clause
 struct FReduce { Ctx c; HD void operator()(u32 i) const { k_reduce_list(c, i); } };
 struct FScores { LcveArgs a; HD void operator()(u32 i) const { k_scores(a, i); } };
 struct FRank { LcveArgs a; HD void operator()(u32 i) const { k_rank(a, i); } };
-struct FMisInit { LcveArgs a; HD void operator()(u32 i) const { k_mis_init(a, i); } };
-struct FMisRound { LcveArgs a; HD void operator()(u32 i) const { k_mis_round(a, i); } };
+struct FMisInit { LcveArgs a; MisList w; HD void operator()(u32 i) const { k_mis_init(a, w, i); } };
+struct FMisRound { LcveArgs a; MisList w; HD void operator()(u32 i) const { k_mis_round(a, w, i); } };
 struct FMisBound { LcveArgs a; HD void operator()(u32 i) const { k_mis_bound(a, i); } };
 struct FElectFlag { LcveArgs a; u32* flags; HD void operator()(u32 i) const { k_elect_flag(a, flags, i); } };
 struct FElectWrite { LcveArgs a; const u32* flags; const u32* scan; HD void operator()(u32 i) const { k_elect_write(a, flags, scan, i); } };
@@ -65,21 +65,6 @@ struct FEre { EreArgs a; HD void operator()(u32 i) const { k_ere_pv(a, i); } };
 struct FEreResolve { EreArgs a; HD void operator()(u32 i) const { k_ere_resolve(a, i); } };
 struct FEreFix { EreArgs a; const u64* keys; u32 n; HD void operator()() const { ere_fixup(a, keys, n); } };
 struct FEreSeq { EreArgs a; HD void operator()() const { ere_sequential(a); } };
-// per-PV working set in bytes (roofline accounting): 4*occ + sum(8 + 4*len)
-struct FPvBytes {
-    Ctx c; const u32* pvs; u64* out;
-    HD void operator()(u32 k) const {
-        const u32 p = V2L(pvs[k]);
-        u64 b = 0;
-        for (u32 side = 0; side < 2; side++) {
-            const u32 l = p + side, o = c.ot_off[l], s = c.ot_size[l];
-            b += 4ull * s;
-            for (u32 i = 0; i < s; i++) b += 8ull + 4ull * c.hdr[c.ot_refs[o + i]].size;
-        }
-        atom_add64(out, b);
-    }
-};
-
 enum Stage { ST_OT = 0, ST_PROP, ST_LCVE, ST_SORT, ST_SUB, ST_VE, ST_BCE, ST_ERE, ST_GC, ST_COUNT, ST_UP, ST_DOWN };
 
 }  // namespace
@@ -136,6 +121,7 @@ struct pf_sigma_ctx {
     pf_round_stats st;
     std::vector<uint32_t> dump;
     u64 alg_bytes = 0;
+    u32 mis_rounds = 0;
 
     Ctx view() {
         Ctx c;
@@ -189,6 +175,7 @@ struct pf_sigma_ctx {
         scan_tmp32.reserve(rt, scan_tmp_elems(n) + 2);
         u32* total = scan_tmp32.p + scan_tmp32.n - 1;
         excl_scan<u32, u32>(in, out, n, total, scan_tmp32.p, rt.stream);
+        rt.launches += 3;
         return read_u32(total);
     }
     template <class Tin>
@@ -196,6 +183,7 @@ struct pf_sigma_ctx {
         scan_tmp64.reserve(rt, scan_tmp_elems(n) + 2);
         u64* total = scan_tmp64.p + scan_tmp64.n - 1;
         excl_scan<Tin, u64>(in, out, n, total, scan_tmp64.p, rt.stream);
+        rt.launches += 3;
         return read_u64(total);
     }
 
@@ -356,17 +344,25 @@ struct pf_sigma_ctx {
         rt.d2d(order_k2.p, score.p + 1, (size_t)nvars * 4);  // keys = score[1..]
         radix_sort_pairs(order_k2.p, order.p, order_v2.p, rank.p, nvars, 32, radix_hist.p, radix_hscan.p,
                          scan_tmp32.p, rt.stream);
+        rt.launches += 20;
         u32 init_b[2] = {NONE, NONE};
         rt.h2d(bound.p, init_b, 8);
         rt.each(FRank{a}, nvars);
-        rt.each(FMisInit{a}, nvars + 1);
-        u32 rounds = 0;
-        while (true) {
+        // work lists: flags / flags_scan (free until the election), resume points: order_v2
+        MisList w{order_v2.p, flags_scan.p, flags.p, counters.p + 3};
+        write_u32(counters.p + 3, 0);
+        rt.each(FMisInit{a, w}, nvars + 1);
+        u32 pending = read_u32(counters.p + 3), rounds = 0;
+        while (pending) {
             if (++rounds > nvars + 2) throw int(PF_ETIMEOUT);
+            const bool in_flags = (w.out == flags.p);  // last round's output is this round's input
+            w.in = in_flags ? flags.p : flags_scan.p;
+            w.out = in_flags ? flags_scan.p : flags.p;
             write_u32(counters.p + 3, 0);
-            rt.each(FMisRound{a}, nvars + 1);
-            if (read_u32(counters.p + 3) == 0) break;
+            rt.each(FMisRound{a, w}, pending);
+            pending = read_u32(counters.p + 3);
         }
+        mis_rounds += rounds;
         rt.d2d(bound.p + 1, bound.p, 4);
         rt.each(FMisBound{a}, nvars + 1);
         rt.each(FFill32{pvrank.p, NONE}, nvars + 1);
@@ -383,15 +379,13 @@ struct pf_sigma_ctx {
     }
 
     void sort_ot() {
-        SortArgs a{view(), pvs.p};
+        rt.zero(counters64.p + 1, 8);
+        SortArgs a{view(), pvs.p, counters64.p + 1};
         rt.each(FSortList{a}, 2 * npvs);
     }
 
-    u64 pv_bytes() {
-        rt.zero(counters64.p + 1, 8);
-        rt.each(FPvBytes{view(), pvs.p, counters64.p + 1}, npvs);
-        return read_u64(counters64.p + 1);
-    }
+    // working set of the elected lists, accumulated by the sort kernel
+    u64 pv_bytes() { return read_u64(counters64.p + 1); }
 
     // SUB (elimination.cpp:110-129).
     void sub() {
@@ -672,7 +666,15 @@ struct pf_sigma_ctx {
     void count_all() {
         rt.zero(counters64.p + 2, 16);
         CountArgs a{view(), counters64.p + 2};
+#if SIGMA_CUDA
+        if (ncls) {
+            rt.launches++;
+            count_live_k<<<rt.grid(ncls, 4), 256, 0, rt.stream>>>(a.c.hdr, ncls, a.out);
+            ck(cudaGetLastError(), "launch");
+        }
+#else
         rt.each(FCount{a}, ncls);
+#endif
         u64 h[2];
         rt.d2h(h, counters64.p + 2, 16);
         n_cls_after = (i64)h[0];
@@ -956,6 +958,7 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     std::memset(&c.st, 0, sizeof(c.st));
     c.dump.clear();
     c.alg_bytes = 0;
+    c.mis_rounds = 0;
     c.rt.launches = 0;
     pf_status status = PF_OK;
     try {
@@ -993,6 +996,7 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     c.st.resolved_words = c.nresolved;
     c.st.algorithmic_bytes = c.alg_bytes;
     c.st.kernel_launches = c.rt.launches;
+    c.st.mis_rounds = c.mis_rounds;
     if (stats) *stats = c.st;
     return status;
 }

@@ -41,7 +41,8 @@ class RoundStats(ctypes.Structure):
                 ("eliminated_vars", ctypes.c_uint64), ("units", ctypes.c_uint64),
                 ("resolved_words", ctypes.c_uint64), ("ms_total", ctypes.c_double),
                 ("ms_stage", ctypes.c_double * 12), ("algorithmic_bytes", ctypes.c_uint64),
-                ("kernel_launches", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 3)]
+                ("kernel_launches", ctypes.c_uint32), ("mis_rounds", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 2)]
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("ms_stage", "reserved")}
