@@ -87,6 +87,22 @@ HD u32 atom_exch(u32* p, u32 v) {
     u32 o = *p; *p = v; return o;
 #endif
 }
+// Add to one counter from many threads: the active lanes of a warp combine their
+// values first, so the counter sees one atomic per warp.
+HD void warp_sum_add64(u64* p, u64 v) {
+#if defined(__CUDA_ARCH__)
+    const unsigned mask = __activemask();
+    if (mask != 0xffffffffu) {  // partial warp (tail of a grid-stride loop): plain atomics
+        atomicAdd((unsigned long long*)p, (unsigned long long)v);
+        return;
+    }
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd((unsigned long long*)p, (unsigned long long)v);
+#else
+    *p += v;
+#endif
+}
+
 // Volatile load for values that other threads of the same launch may update.
 HD u32 vload(const u32* p) { return *(const volatile u32*)p; }
 

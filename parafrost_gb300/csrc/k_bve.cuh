@@ -13,18 +13,15 @@
 // Units go straight to the trail through a compare-and-swap on their variable.
 //
 // Elected variables share no clause, so molten flags and in-place edits stay
-// private. Gate finders also read lists of neighbour literals (never elected);
-// where the reference takes the first match of such a list (which it keeps in
-// clause-store order) the smallest matching clause id is taken instead.
+// private. The decision lives in k_bve_analyze.cuh.
 #pragma once
 
 #include "cnf.cuh"
 #include "introsort.cuh"
+#include "k_bve_analyze.cuh"
 #include "k_sub.cuh"
 
 namespace sigma {
-
-enum : uint8_t { VE_KEEP = 0, VE_PURE = 1, VE_EQU = 2, VE_RES = 3, VE_SUBST = 4 };
 
 struct BveArgs {
     Ctx c;
@@ -64,41 +61,6 @@ HD ListRef list_of(const Ctx& c, u32 l) {
     return r;
 }
 
-HD u32 count_orgs(const Ctx& c, u32 l) {
-    const ListRef L = list_of(c, l);
-    u32 n = 0;
-    for (u32 i = 0; i < L.n; i++) if (h_original(c.hdr[L.ids[i]].flags)) n++;
-    return n;
-}
-
-HD u32 lits_before(const Ctx& c, u32 l) {
-    const ListRef L = list_of(c, l);
-    u32 n = 0;
-    for (u32 i = 0; i < L.n; i++) {
-        const Hdr h = c.hdr[L.ids[i]];
-        if (h_original(h.flags)) n += h.size;
-    }
-    return n;
-}
-
-// merge(x, c1, c2) -> resolvent size, 0 for a tautology (simplify.h:175-202).
-HD int merge_size(u32 x, const u32* a, u32 n1, const u32* b, u32 n2) {
-    u32 i = 0, j = 0;
-    int len = (int)(n1 + n2) - 2;
-    while (i < n1 && j < n2) {
-        const u32 l1 = a[i], l2 = b[j];
-        const u32 v1 = ABS(l1), v2 = ABS(l2);
-        if (v1 == x) i++;
-        else if (v2 == x) j++;
-        else if ((l1 ^ l2) == 1u) return 0;
-        else if (v1 < v2) i++;
-        else if (v2 < v1) j++;
-        else { i++; j++; len--; }
-    }
-    return len;
-}
-
-// merge(x, c1, c2, out) (simplify.h:139-173); false for a tautology.
 HD bool merge_into(u32 x, const u32* a, u32 n1, const u32* b, u32 n2, u32* out, u32& on) {
     u32 i = 0, j = 0;
     on = 0;
@@ -117,344 +79,46 @@ HD bool merge_into(u32 x, const u32* a, u32 n1, const u32* b, u32 n2, u32* out, 
     return true;
 }
 
-// countResolvents / countSubstituted (simplify.h:237-295). Returns true when the
-// elimination is rejected; nAdded/nLits hold the counts (exact when accepted).
-HD bool count_added(const BveArgs& a, u32 x, int clsbefore, u32 lme, u32 lother, int& nAdded, u32& nLits, bool gate) {
-    const Ctx& c = a.c;
-    const ListRef me = list_of(c, lme), other = list_of(c, lother);
-    u32 added_lits = 0;
-    const int rlimit = a.ve_clause_max;
-    for (u32 i = 0; i < me.n; i++) {
-        const Hdr hi = c.hdr[me.ids[i]];
-        if (!h_original(hi.flags)) continue;
-        const bool mi = h_molten(hi.flags);
-        const u32* li = c.lits + hi.start;
-        for (u32 j = 0; j < other.n; j++) {
-            const Hdr hj = c.hdr[other.ids[j]];
-            if (!h_original(hj.flags)) continue;
-            if (gate && mi == h_molten(hj.flags)) continue;
-            const int rsize = merge_size(x, li, hi.size, c.lits + hj.start, hj.size);
-            if (rsize > 1) {
-                if (++nAdded > clsbefore || (rlimit && rsize > rlimit)) { nLits = added_lits; return true; }
-                added_lits += (u32)rsize;
-            }
-        }
-    }
-    nLits = added_lits;
-    if (a.ve_lbound) {
-        if (added_lits > lits_before(c, lme) + lits_before(c, lother)) return true;
-    }
-    return false;
-}
-
-HD void freeze_binaries(const Ctx& c, u32 l) {
-    const ListRef L = list_of(c, l);
-    for (u32 i = 0; i < L.n; i++) {
-        const u32 r = L.ids[i];
-        const Hdr h = c.hdr[r];
-        if (h_original(h.flags) && h.size == 2) set_molten(c, r, false);
-    }
-}
-
-// ---------------------------------------------------------------- EQU
-// find_sfanin + find_BN_gate (equivalence.h:88-130).
-HD u32 find_bn_gate(const Ctx& c, u32 p) {
-    const u32 n = NEG(p);
-    u32 first = 0;
-    {
-        const ListRef L = list_of(c, p);
-        u32 imp = 0;
-        int nImps = 0;
-        bool multi = false;
-        for (u32 i = 0; i < L.n; i++) {
-            const u32 r = L.ids[i];
-            const Hdr h = c.hdr[r];
-            if (h_original(h.flags) && h.size == 2) {
-                const u32* l = c.lits + h.start;
-                imp = FLIP(l[0] ^ l[1] ^ p);
-                set_molten(c, r, true);
-                nImps++;
-            }
-            if (nImps > 1) { multi = true; break; }
-        }
-        first = multi ? 0u : imp;
-    }
-    if (first) {
-        u32 second = n, def = first;
-        if (second < first) { first = second; second = def; }
-        const ListRef N = list_of(c, n);
-        for (u32 i = 0; i < N.n; i++) {
-            const u32 r = N.ids[i];
-            const Hdr h = c.hdr[r];
-            if (!(h_original(h.flags) && h.size == 2)) continue;
-            const u32* l = c.lits + h.start;
-            if (l[0] == first && l[1] == second) {
-                set_molten(c, r, true);
-                return def;
-            }
-        }
-    }
-    freeze_binaries(c, p);
-    return 0;
-}
-
-// ---------------------------------------------------------------- AND/OR
-// find_fanin + find_AO_gate (and.h:25-86). out: scratch of at least |ot[dx]|+1 words.
-HD bool find_ao_gate(const BveArgs& a, u32 dx, int nOrgCls, u32* out, int& nAdded, u32& nLits) {
-    const Ctx& c = a.c;
-    const u32 x = ABS(dx);
-    const ListRef I = list_of(c, dx);
-    u32 on = 0, sig = 0;
-    for (u32 i = 0; i < I.n; i++) {
-        const u32 r = I.ids[i];
-        const Hdr h = c.hdr[r];
-        if (h_original(h.flags) && h.size == 2) {
-            const u32* l = c.lits + h.start;
-            const u32 imp = FLIP(l[0] ^ l[1] ^ dx);
-            out[on++] = imp;
-            sig |= MAPHASH(imp);
-            set_molten(c, r, true);
-        }
-    }
-    if (on > 1) {
-        const u32 f_dx = FLIP(dx);
-        out[on++] = f_dx;
-        sig |= MAPHASH(f_dx);
-        reference_list_sort(out, (int)on, LitLess());
-        const ListRef O = list_of(c, f_dx);
-        for (u32 i = 0; i < O.n; i++) {
-            const u32 r = O.ids[i];
-            const Hdr h = c.hdr[r];
-            if (!(h_original(h.flags) && h.size == on && sig_sub(h.sig, sig))) continue;
-            const u32* l = c.lits + h.start;
-            bool eq = true;
-            for (u32 t = 0; t < on; t++) if (l[t] != out[t]) { eq = false; break; }
-            if (!eq) continue;
-            set_molten(c, r, true);
-            nAdded = 0;
-            if (count_added(a, x, nOrgCls, dx, f_dx, nAdded, nLits, true)) {
-                set_molten(c, r, false);
-                break;
-            }
-            return true;
-        }
-    }
-    freeze_binaries(c, dx);
-    return false;
-}
-
-// ---------------------------------------------------------------- ITE
-// fast_equality_check (ifthenelse.h:25-40): the original, unmolten ternary (x y z)
-// in the shortest of the three lists; NONE if absent. The first argument is always
-// the elected variable's own literal, so every clause that can match is in that
-// literal's own list: the search scans the own list and returns the first match in
-// its order when the reference picks the own list, else the smallest matching id
-// (the reference's first match in a neighbour list, which it keeps in clause-store
-// order, among the same set of live matching clauses).
-HD u32 fast_equality_check(const Ctx& c, u32 v, u32 x, u32 y, u32 z) {
-    const u32 ownlit = x;
-    if (c.ot_size[y] > c.ot_size[z]) swap_t(y, z);
-    if (c.ot_size[x] > c.ot_size[y]) swap_t(x, y);
-    const u32 ll = x;
-    // sort3 (simplify.h:105-117)
-    { const u32 lo = y < z ? y : z, hi = y < z ? z : y; y = lo; z = hi; }
-    { const u32 lo = x < z ? x : z, hi = x < z ? z : x; x = lo; z = hi; }
-    { const u32 lo = x < y ? x : y, hi = x < y ? y : x; x = lo; y = hi; }
-    const ListRef L = list_of(c, ownlit);
-    const bool own = ll == ownlit;
-    (void)v;
-    u32 best = NONE;
-    for (u32 i = 0; i < L.n; i++) {
-        const u32 r = L.ids[i];
-        const Hdr h = c.hdr[r];
-        if (h_molten(h.flags)) continue;
-        if (!(h_original(h.flags) && h.size == 3)) continue;
-        const u32* l = c.lits + h.start;
-        if (l[0] == x && l[1] == y && l[2] == z) {
-            if (own) return r;
-            if (r < best) best = r;
-        }
-    }
-    return best;
-}
-
-// find_ITE_gate (ifthenelse.h:42-97).
-HD bool find_ite_gate(const BveArgs& a, u32 dx, int nOrgCls, int& nAdded, u32& nLits) {
-    const Ctx& c = a.c;
-    const u32 fx = FLIP(dx), v = ABS(dx);
-    const ListRef I = list_of(c, dx);
-    for (u32 i = 0; i < I.n; i++) {
-        const u32 ri = I.ids[i];
-        const Hdr hi = c.hdr[ri];
-        if (!(h_original(hi.flags) && hi.size == 3)) continue;
-        const u32* li = c.lits + hi.start;
-        u32 xi = li[0], yi = li[1], zi = li[2];
-        if (yi == dx) swap_t(xi, yi);
-        if (zi == dx) swap_t(xi, zi);
-        for (u32 j = i + 1; j < I.n; j++) {
-            const u32 rj = I.ids[j];
-            const Hdr hj = c.hdr[rj];
-            if (!(h_original(hj.flags) && hj.size == 3)) continue;
-            const u32* lj = c.lits + hj.start;
-            u32 xj = lj[0], yj = lj[1], zj = lj[2];
-            if (yj == dx) swap_t(xj, yj);
-            if (zj == dx) swap_t(xj, zj);
-            if (ABS(yi) == ABS(zj)) swap_t(yj, zj);
-            if (ABS(zi) == ABS(zj)) continue;
-            if (yi != FLIP(yj)) continue;
-            const u32 d1 = fast_equality_check(c, v, fx, yi, FLIP(zi));
-            if (d1 == NONE) continue;
-            const u32 d2 = fast_equality_check(c, v, fx, yj, FLIP(zj));
-            if (d2 == NONE) continue;
-            set_molten(c, ri, true); set_molten(c, rj, true);
-            set_molten(c, d1, true); set_molten(c, d2, true);
-            nAdded = 0;
-            if (count_added(a, v, nOrgCls, dx, fx, nAdded, nLits, true)) {
-                set_molten(c, ri, false); set_molten(c, rj, false);
-                set_molten(c, d1, false); set_molten(c, d2, false);
-                return false;
-            }
-            return true;
-        }
-    }
-    return false;
-}
-
-// ---------------------------------------------------------------- XOR
-constexpr int XOR_MAX_SIZE = 21;  // xormaxarity <= 20 (src/cpu/options.cpp:46)
-
-HD void freeze_arities(const Ctx& c, u32 l1, u32 l2) {
-    for (u32 side = 0; side < 2; side++) {
-        const ListRef L = list_of(c, side ? l2 : l1);
-        for (u32 i = 0; i < L.n; i++) {
-            const u32 r = L.ids[i];
-            const Hdr h = c.hdr[r];
-            if (h.size > 2 && h_molten(h.flags)) set_molten(c, r, false);
-        }
-    }
-}
-
-// makeArity (xor.h:52-84), COUNTFLIPS (xor.h:23-27).
-HD bool make_arity(const Ctx& c, u32 v, u32& parity, u32* lits, int size) {
-    const u32 oldparity = parity;
-    do { ++parity; } while (popc32(parity) & 1);
-    for (int k = 0; k < size; k++) {
-        const u32 bit = 1u << k;
-        if ((parity & bit) != (oldparity & bit)) lits[k] = FLIP(lits[k]);
-    }
-    u32 best = lits[0];
-    u32 minsize = c.ot_size[best];
-    u32 ownlit = lits[0];
-    for (int k = 1; k < size; k++) {
-        const u32 ls = c.ot_size[lits[k]];
-        if (ls < minsize) { minsize = ls; best = lits[k]; }
-    }
-    for (int k = 0; k < size; k++) if (ABS(lits[k]) == v) ownlit = lits[k];
-    // Every clause that can match holds the variable's own literal: scan that list
-    // (see fast_equality_check for why the result is the reference's).
-    const ListRef L = list_of(c, ownlit);
-    const bool own = best == ownlit;
-    u32 found = NONE;
-    for (u32 i = 0; i < L.n; i++) {
-        const u32 r = L.ids[i];
-        const Hdr h = c.hdr[r];
-        if (!(h_original(h.flags) && h.size == (u32)size)) continue;
-        const u32* l = c.lits + h.start;
-        bool all = true;
-        for (int t = 0; t < size && all; t++) {  // checkArity (xor.h:35-50)
-            bool in = false;
-            for (int q = 0; q < size; q++) if (l[t] == lits[q]) { in = true; break; }
-            all = in;
-        }
-        if (!all) continue;
-        if (own) { found = r; break; }
-        if (r < found) found = r;
-    }
-    if (found == NONE) return false;
-    set_molten(c, found, true);
-    return true;
-}
-
-// find_XOR_gate (xor.h:86-131).
-HD bool find_xor_gate(const BveArgs& a, u32 dx, int nOrgCls, int& nAdded, u32& nLits) {
-    const Ctx& c = a.c;
-    const u32 fx = FLIP(dx), v = ABS(dx);
-    const ListRef I = list_of(c, dx);
-    u32 out[XOR_MAX_SIZE];
-    for (u32 i = 0; i < I.n; i++) {
-        const u32 ri = I.ids[i];
-        const Hdr hi = c.hdr[ri];
-        if (!h_original(hi.flags)) continue;
-        const int size = (int)hi.size;
-        const int arity = size - 1;
-        if (size < 3 || arity > a.xor_max_arity) continue;
-        const u32* li = c.lits + hi.start;
-        for (int t = 0; t < size; t++) out[t] = li[t];
-        u32 parity = 0;
-        int itargets = 1 << arity;
-        while (--itargets && make_arity(c, v, parity, out, size)) {}
-        if (itargets) freeze_arities(c, dx, fx);
-        else {
-            set_molten(c, ri, true);
-            nAdded = 0;
-            if (count_added(a, v, nOrgCls, dx, fx, nAdded, nLits, true)) {
-                freeze_arities(c, dx, fx);
-                break;
-            }
-            return true;
-        }
-    }
-    return false;
-}
-
-// Witness words of toblivion / save_BN_gate (simplify.h:305-332, equivalence.h:132-153).
-HD u32 witness_words(const Ctx& c, u32 p, u32 pOrgs, u32 nOrgs) {
-    const u32 l = pOrgs > nOrgs ? NEG(p) : p;
-    const ListRef L = list_of(c, l);
-    u32 w = 2;
-    for (u32 i = 0; i < L.n; i++) {
-        const Hdr h = c.hdr[L.ids[i]];
-        if (h_original(h.flags)) w += h.size + 1;
-    }
-    return w;
-}
-
-// Step 1: the decision of bve() (bve.cpp:37-142) for one elected variable.
-HD void k_bve_analyze(const BveArgs& a, u32 k) {
-    const Ctx& c = a.c;
-    const u32 v = a.pvs[k];
-    const u32 p = V2L(v), n = NEG(p);
-    const u32 pOrgs = count_orgs(c, p), nOrgs = count_orgs(c, n);
-    uint8_t type = VE_KEEP;
-    int nAdded = 0;
-    u32 nLits = 0, def = 0;
-    if (!pOrgs || !nOrgs) {
-        type = VE_PURE;
-    } else if ((def = find_bn_gate(c, p)) != 0) {
-        type = VE_EQU;
+// Step 1 for one elected variable: the decision on a shared-memory copy of its lists
+// when they fit the slot, else on global memory.
+HD void bve_analyze_one(const BveArgs& a, u32 k, u32* slot) {
+    VeOpts o;
+    o.ve_clause_max = a.ve_clause_max;
+    o.ve_lbound = a.ve_lbound;
+    o.xor_max_arity = a.xor_max_arity;
+    VeResult r;
+    SmemPv s;
+    if (s.stage(a.c, a.pvs[k], slot)) {
+        r = pv_bve_decide(s, o);
     } else {
-        const int nOrgCls = (int)(pOrgs + nOrgs);
-        u32* scr = a.scr + a.scr_off[k];
-        if (nOrgCls > 2) {
-            if (find_ao_gate(a, n, nOrgCls, scr, nAdded, nLits)) type = VE_SUBST;
-            else if (!nAdded && find_ao_gate(a, p, nOrgCls, scr, nAdded, nLits)) type = VE_SUBST;
-        }
-        if (type == VE_KEEP && nOrgCls > 3) {
-            if (find_ite_gate(a, p, nOrgCls, nAdded, nLits)) type = VE_SUBST;
-            else if (!nAdded && find_ite_gate(a, n, nOrgCls, nAdded, nLits)) type = VE_SUBST;
-            else if (find_xor_gate(a, p, nOrgCls, nAdded, nLits)) type = VE_SUBST;
-            else if (!nAdded && find_xor_gate(a, n, nOrgCls, nAdded, nLits)) type = VE_SUBST;
-        }
-        if (type == VE_KEEP && !nAdded && !count_added(a, v, nOrgCls, p, n, nAdded, nLits, false)) type = VE_RES;
+        GlobalPv g;
+        g.init(a.c, a.pvs[k], a.scr + a.scr_off[k]);
+        r = pv_bve_decide(g, o);
     }
-    a.type[k] = type;
-    a.porgs[k] = pOrgs;
-    a.norgs[k] = nOrgs;
-    a.def[k] = def;
-    const bool adds = type == VE_RES || type == VE_SUBST;
-    a.ncls[k] = adds ? (u32)nAdded : 0u;
-    a.nlits[k] = adds ? nLits : 0u;
-    a.nwit[k] = type == VE_KEEP ? 0u : witness_words(c, p, pOrgs, nOrgs);
+    a.type[k] = r.type;
+    a.porgs[k] = r.porgs;
+    a.norgs[k] = r.norgs;
+    a.def[k] = r.def;
+    a.ncls[k] = r.ncls;
+    a.nlits[k] = r.nlits;
+    a.nwit[k] = r.nwit;
+}
+
+#if SIGMA_CUDA
+// One thread per elected variable, PV_SLOT words of shared memory per thread.
+constexpr int kBveThreads = 128;
+__global__ void __launch_bounds__(kBveThreads) bve_analyze_k(BveArgs a) {
+    extern __shared__ u32 smem[];
+    u32* slot = smem + threadIdx.x * PV_SLOT;
+    for (u32 k = blockIdx.x * blockDim.x + threadIdx.x; k < a.npvs; k += gridDim.x * blockDim.x)
+        bve_analyze_one(a, k, slot);
+}
+#endif
+
+// Emulation entry: the slot is a local array.
+HD void k_bve_analyze(const BveArgs& a, u32 k) {
+    u32 slot[PV_SLOT];
+    bve_analyze_one(a, k, slot);
 }
 
 // ---------------------------------------------------------------- write step

@@ -61,7 +61,7 @@ HD void k_rank(const LcveArgs& a, u32 p) {
 // resumes there. Indices are capped, which only makes a scan start earlier.
 struct MisList {
     u32* resume;
-    const u32* in;
+    u32* in;
     u32* out;
     u32* nout;
 };
@@ -71,12 +71,18 @@ HD u32 mis_pos(u32 side, u32 i, u32 k) {
     return (side << 31) | (i << 8) | (k < 255u ? k : 255u);
 }
 
-HD void k_mis_init(const LcveArgs& a, const MisList& w, u32 v) {
+// Vertices whose two lists hold more than this many clauses are scanned by a whole
+// warp (one clause per lane) instead of one thread.
+constexpr u32 MIS_WARP_MIN_OCC = 12;
+
+HD void k_mis_init(const LcveArgs& a, const MisList& small, const MisList& big, u32 v) {
     if (v == 0) { a.state[0] = MIS_NONE; return; }
     const bool in_graph = lcve_valid(a.c, v) && lcve_freezable(a, v) && a.rank[v] < a.bound[0];
     a.state[v] = in_graph ? MIS_UNDECIDED : MIS_NONE;
     if (in_graph) {
-        w.resume[v] = 0;
+        small.resume[v] = 0;
+        const u32 occ = a.c.ot_size[V2L(v)] + a.c.ot_size[NEG(V2L(v))];
+        const MisList& w = occ > MIS_WARP_MIN_OCC ? big : small;
         w.out[atom_add(w.nout, 1u)] = v;
     }
 }
@@ -116,6 +122,64 @@ HD void k_mis_round(const LcveArgs& a, const MisList& w, u32 idx) {
         w.out[atom_add(w.nout, 1u)] = v;
     }
 }
+
+#if SIGMA_CUDA
+// The same round with one warp per vertex: lanes take consecutive clauses of the
+// two lists (from the resume point, at clause granularity), ballots give "some lower
+// neighbour is in" and the first clause holding an undecided lower neighbour.
+__global__ void mis_round_warp_k(LcveArgs a, MisList w, u32 n) {
+    const u32 lane = threadIdx.x & 31u;
+    const u32 nwarps = (gridDim.x * blockDim.x) >> 5;
+    volatile uint8_t* st = (volatile uint8_t*)a.state;
+    const Ctx& c = a.c;
+    for (u32 idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < n; idx += nwarps) {
+        const u32 v = w.in[idx];
+        if (st[v] != MIS_UNDECIDED) continue;
+        const u32 rv = a.rank[v];
+        const u32 pos = w.resume[v];
+        const u32 side0 = pos >> 31, i0 = (pos >> 8) & 0x7FFFFFu;
+        const u32 np = c.ot_size[V2L(v)], nn = c.ot_size[NEG(V2L(v))];
+        const u32 op = c.ot_off[V2L(v)], on = c.ot_off[NEG(V2L(v))];
+        const u32 total = np + nn;
+        const u32 t0 = side0 ? np + (i0 < nn ? i0 : nn) : (i0 < np ? i0 : np);
+        u32 first = NONE;
+        bool out = false;
+        for (u32 base = t0; base < total; base += 32) {
+            const u32 t = base + lane;
+            bool has_in = false, has_und = false;
+            if (t < total) {
+                const Hdr h = c.hdr[c.ot_refs[t < np ? op + t : on + (t - np)]];
+                if (!h_deleted(h.flags)) {
+                    const u32* L = c.lits + h.start;
+                    for (u32 k = 0; k < h.size; k++) {
+                        const u32 u = ABS(L[k]);
+                        if (u == v) continue;
+                        const uint8_t su = st[u];
+                        if (su == MIS_NONE || a.rank[u] > rv) continue;
+                        if (su == MIS_IN) { has_in = true; break; }
+                        if (su == MIS_UNDECIDED) has_und = true;
+                    }
+                }
+            }
+            if (__ballot_sync(0xffffffffu, has_in)) { out = true; break; }
+            const u32 und = __ballot_sync(0xffffffffu, has_und);
+            if (und && first == NONE) {
+                const u32 tt = base + (u32)(__ffs(und) - 1);
+                first = tt < np ? mis_pos(0, tt, 0) : mis_pos(1, tt - np, 0);
+            }
+        }
+        if (lane == 0) {
+            if (out) st[v] = MIS_OUT;
+            else if (first == NONE) st[v] = MIS_IN;
+            else {
+                w.resume[v] = first;
+                w.out[atomicAdd(w.nout, 1u)] = v;
+            }
+        }
+        __syncwarp();
+    }
+}
+#endif
 
 // B = min(B0, first member whose lists reach the temperatures).
 HD void k_mis_bound(const LcveArgs& a, u32 v) {

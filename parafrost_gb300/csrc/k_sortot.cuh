@@ -42,7 +42,7 @@ HD void k_sort_list(const SortArgs& a, u32 k) {
     u32* d = a.c.ot_refs + a.c.ot_off[l];
     u64 ws = 4ull * n;
     for (u32 i = 0; i < n; i++) ws += 8ull + 4ull * a.c.hdr[d[i]].size;
-    atom_add64(a.ws_bytes, ws);
+    warp_sum_add64(a.ws_bytes, ws);
     if (n <= 1) return;
     if (n <= 20) ref_insertion_sort(d, (int)n, IdLess());
     else std_sort_replica(d, d + n, IdLess());

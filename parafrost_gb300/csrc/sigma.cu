@@ -42,7 +42,7 @@ struct FPropClause { PropArgs a; HD void operator()(u32 i) const { k_prop_clause
 struct FReduce { Ctx c; HD void operator()(u32 i) const { k_reduce_list(c, i); } };
 struct FScores { LcveArgs a; HD void operator()(u32 i) const { k_scores(a, i); } };
 struct FRank { LcveArgs a; HD void operator()(u32 i) const { k_rank(a, i); } };
-struct FMisInit { LcveArgs a; MisList w; HD void operator()(u32 i) const { k_mis_init(a, w, i); } };
+struct FMisInit { LcveArgs a; MisList s, b; HD void operator()(u32 i) const { k_mis_init(a, s, b, i); } };
 struct FMisRound { LcveArgs a; MisList w; HD void operator()(u32 i) const { k_mis_round(a, w, i); } };
 struct FMisBound { LcveArgs a; HD void operator()(u32 i) const { k_mis_bound(a, i); } };
 struct FElectFlag { LcveArgs a; u32* flags; HD void operator()(u32 i) const { k_elect_flag(a, flags, i); } };
@@ -94,6 +94,7 @@ struct pf_sigma_ctx {
     // stage scratch
     DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
     DBuf<uint8_t> mis_state;
+    DBuf<u32> mis_big_a, mis_big_b;
     DBuf<u32> work, cl_stamp;
     DBuf<u32> radix_hist, radix_hscan, scan_tmp32;
     DBuf<u64> scan_tmp64;
@@ -348,19 +349,35 @@ struct pf_sigma_ctx {
         u32 init_b[2] = {NONE, NONE};
         rt.h2d(bound.p, init_b, 8);
         rt.each(FRank{a}, nvars);
-        // work lists: flags / flags_scan (free until the election), resume points: order_v2
-        MisList w{order_v2.p, flags_scan.p, flags.p, counters.p + 3};
+        // work lists of undecided vertices, small and large adjacency (ping-pong pairs);
+        // resume points in order_v2 (free after the sort)
+        mis_big_a.reserve(rt, nvars + 1);
+        mis_big_b.reserve(rt, nvars + 1);
+        MisList ws{order_v2.p, flags_scan.p, flags.p, counters.p + 3};
+        MisList wb{order_v2.p, mis_big_b.p, mis_big_a.p, counters.p + 10};
         write_u32(counters.p + 3, 0);
-        rt.each(FMisInit{a, w}, nvars + 1);
-        u32 pending = read_u32(counters.p + 3), rounds = 0;
-        while (pending) {
+        write_u32(counters.p + 10, 0);
+        rt.each(FMisInit{a, ws, wb}, nvars + 1);
+        u32 pend_s = read_u32(counters.p + 3), pend_b = read_u32(counters.p + 10), rounds = 0;
+        while (pend_s || pend_b) {
             if (++rounds > nvars + 2) throw int(PF_ETIMEOUT);
-            const bool in_flags = (w.out == flags.p);  // last round's output is this round's input
-            w.in = in_flags ? flags.p : flags_scan.p;
-            w.out = in_flags ? flags_scan.p : flags.p;
+            // last round's output list is this round's input
+            std::swap(ws.out, ws.in);
+            std::swap(wb.out, wb.in);
             write_u32(counters.p + 3, 0);
-            rt.each(FMisRound{a, w}, pending);
-            pending = read_u32(counters.p + 3);
+            write_u32(counters.p + 10, 0);
+            if (pend_s) rt.each(FMisRound{a, ws}, pend_s);
+            if (pend_b) {
+#if SIGMA_CUDA
+                rt.launches++;
+                mis_round_warp_k<<<rt.grid(pend_b * 32u, 8), 256, 0, rt.stream>>>(a, wb, pend_b);
+                ck(cudaGetLastError(), "launch");
+#else
+                rt.each(FMisRound{a, wb}, pend_b);
+#endif
+            }
+            pend_s = read_u32(counters.p + 3);
+            pend_b = read_u32(counters.p + 10);
         }
         mis_rounds += rounds;
         rt.d2d(bound.p + 1, bound.p, 4);
@@ -568,7 +585,24 @@ struct pf_sigma_ctx {
         a.def = ve_def.p;
         a.scr_off = ve_scr_off.p;
         a.scr = ve_scr.p;
+#if SIGMA_CUDA
+        {
+            const int smem = kBveThreads * (int)PV_SLOT * 4;
+            static bool attr_set = false;
+            if (!attr_set) {
+                ck(cudaFuncSetAttribute(bve_analyze_k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "smem attr");
+                attr_set = true;
+            }
+            u32 blocks = (npvs + kBveThreads - 1) / kBveThreads;
+            const u32 cap = (u32)rt.sms * 3u;
+            if (blocks > cap) blocks = cap;
+            rt.launches++;
+            bve_analyze_k<<<blocks, kBveThreads, smem, rt.stream>>>(a);
+            ck(cudaGetLastError(), "launch");
+        }
+#else
         rt.each(FBveAnalyze{a}, npvs);
+#endif
         check();
         const u32 add_cls = scan32(ve_ncls.p, ve_cls_scan.p, npvs);
         const u64 add_lits = scan64(ve_nlits.p, ve_lit_scan.p, npvs);
@@ -1177,6 +1211,8 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
                         &c.ve_wit_scan, &c.sub_wrd, &c.sub_wrd_off, &c.ere_claim, &c.ere_key};
     for (auto* b : b64) b->free();
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.mis_state, &c.ve_type, &c.sub_run};
+    c.mis_big_a.free();
+    c.mis_big_b.free();
     for (auto* b : b8) b->free();
     c.sub_units.free();
     c.sub_pairs.free();
