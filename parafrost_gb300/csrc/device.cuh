@@ -103,6 +103,27 @@ HD void warp_sum_add64(u64* p, u64 v) {
 #endif
 }
 
+// Append to a list through one shared counter: the lanes of a warp that append
+// reserve their slots with one atomic. Returns the slot (only meaningful when pred).
+HD u32 warp_append(u32* counter, bool pred) {
+#if defined(__CUDA_ARCH__)
+    const unsigned mask = __activemask();
+    const unsigned bal = __ballot_sync(mask, pred);
+    if (!bal) return 0;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(bal) - 1;
+    u32 base = 0;
+    if (lane == leader) base = atomicAdd(counter, (u32)__popc(bal));
+    base = __shfl_sync(mask, base, leader);
+    return base + (u32)__popc(bal & ((1u << lane) - 1u));
+#else
+    if (!pred) return 0;
+    const u32 o = *counter;
+    *counter = o + 1;
+    return o;
+#endif
+}
+
 // Volatile load for values that other threads of the same launch may update.
 HD u32 vload(const u32* p) { return *(const volatile u32*)p; }
 

@@ -79,12 +79,12 @@ HD void k_mis_init(const LcveArgs& a, const MisList& small, const MisList& big, 
     if (v == 0) { a.state[0] = MIS_NONE; return; }
     const bool in_graph = lcve_valid(a.c, v) && lcve_freezable(a, v) && a.rank[v] < a.bound[0];
     a.state[v] = in_graph ? MIS_UNDECIDED : MIS_NONE;
-    if (in_graph) {
-        small.resume[v] = 0;
-        const u32 occ = a.c.ot_size[V2L(v)] + a.c.ot_size[NEG(V2L(v))];
-        const MisList& w = occ > MIS_WARP_MIN_OCC ? big : small;
-        w.out[atom_add(w.nout, 1u)] = v;
-    }
+    if (in_graph) small.resume[v] = 0;
+    const bool is_big = in_graph && a.c.ot_size[V2L(v)] + a.c.ot_size[NEG(V2L(v))] > MIS_WARP_MIN_OCC;
+    const u32 ps = warp_append(small.nout, in_graph && !is_big);
+    const u32 pb = warp_append(big.nout, is_big);
+    if (in_graph && !is_big) small.out[ps] = v;
+    if (is_big) big.out[pb] = v;
 }
 
 // One round for an undecided vertex: scan its live clauses from the resume point.
@@ -119,7 +119,7 @@ HD void k_mis_round(const LcveArgs& a, const MisList& w, u32 idx) {
         st[v] = MIS_IN;
     } else {
         w.resume[v] = first;
-        w.out[atom_add(w.nout, 1u)] = v;
+        w.out[warp_append(w.nout, true)] = v;
     }
 }
 
