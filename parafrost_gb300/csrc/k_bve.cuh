@@ -88,7 +88,7 @@ HD void bve_analyze_one(const BveArgs& a, u32 k, u32* slot) {
     o.xor_max_arity = a.xor_max_arity;
     VeResult r;
     SmemPv s;
-    if (s.stage(a.c, a.pvs[k], slot)) {
+    if (slot && s.stage(a.c, a.pvs[k], slot)) {
         r = pv_bve_decide(s, o);
     } else {
         GlobalPv g;
@@ -105,17 +105,25 @@ HD void bve_analyze_one(const BveArgs& a, u32 k, u32* slot) {
 }
 
 #if SIGMA_CUDA
-// One thread per elected variable, PV_SLOT words of shared memory per thread.
+// One thread per elected variable, PV_SLOT words of shared memory per thread, warps
+// taking 32 variables at a time in work order (perm) from a shared counter.
 constexpr int kBveThreads = 128;
-__global__ void __launch_bounds__(kBveThreads) bve_analyze_k(BveArgs a) {
+__global__ void __launch_bounds__(kBveThreads) bve_analyze_k(BveArgs a, const u32* perm, u32* next) {
     extern __shared__ u32 smem[];
     u32* slot = smem + threadIdx.x * PV_SLOT;
-    for (u32 k = blockIdx.x * blockDim.x + threadIdx.x; k < a.npvs; k += gridDim.x * blockDim.x)
-        bve_analyze_one(a, k, slot);
+    const u32 lane = threadIdx.x & 31u;
+    while (true) {
+        u32 base = 0;
+        if (lane == 0) base = atomicAdd(next, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= a.npvs) break;
+        if (base + lane < a.npvs) bve_analyze_one(a, perm[base + lane], slot);
+        __syncwarp();
+    }
 }
 #endif
 
-// Emulation entry: the slot is a local array.
+// Emulation entry of the staged path: the slot is a local array.
 HD void k_bve_analyze(const BveArgs& a, u32 k) {
     u32 slot[PV_SLOT];
     bve_analyze_one(a, k, slot);

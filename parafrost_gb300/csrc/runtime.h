@@ -36,6 +36,21 @@ template <class F>
 __global__ void for_each_k(F f, u32 n) {
     for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += blockDim.x * gridDim.x) f(i);
 }
+// Dynamic scheduling: every warp takes the next 32 items from a shared counter until
+// none are left, so long items do not leave most SMs idle at the end.
+template <class F>
+__global__ void for_each_dyn_k(F f, u32 n, u32* next) {
+    const u32 lane = threadIdx.x & 31u;
+    while (true) {
+        u32 base = 0;
+        if (lane == 0) base = atomicAdd(next, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const u32 i = base + lane;
+        if (i < n) f(i);
+        __syncwarp();
+    }
+}
 template <class F>
 __global__ void single_k(F f) {
     if (blockIdx.x == 0 && threadIdx.x == 0) f();
@@ -140,6 +155,24 @@ struct Runtime {
         for_each_k<F><<<grid(n), 256, 0, stream>>>(f, n);
         ck(cudaGetLastError(), "launch");
 #else
+        for (u32 i = 0; i < n; i++) f(i);
+#endif
+    }
+    // f(i) for i in [0, n) with dynamic warp-chunk scheduling; `next` is a device
+    // counter the call resets.
+    template <class F>
+    void each_dyn(const F& f, u32 n, u32* next) {
+        if (!n) return;
+        launches++;
+#if SIGMA_CUDA
+        ck(cudaMemsetAsync(next, 0, 4, stream), "memset");
+        u32 g = (u32)sms * 8u;
+        const u32 need = (n + 255u) / 256u;
+        if (g > need) g = need;
+        for_each_dyn_k<F><<<g, 256, 0, stream>>>(f, n, next);
+        ck(cudaGetLastError(), "launch");
+#else
+        (void)next;
         for (u32 i = 0; i < n; i++) f(i);
 #endif
     }

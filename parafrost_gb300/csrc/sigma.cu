@@ -57,7 +57,8 @@ struct FSubRestore { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_rest
 struct FSubReach { SubReachArgs a; HD void operator()(u32 i) const { k_sub_reach(a, i); } };
 struct FSubCommit { Ctx c; const u32* lits; HD void operator()(u32 i) const { k_sub_commit_oblivion(c, lits, i); } };
 struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) const { k_bve_scratch_need(c, pvs, need, i); } };
-struct FBveAnalyze { BveArgs a; HD void operator()(u32 i) const { k_bve_analyze(a, i); } };
+struct FBveAnalyze { BveArgs a; HD void operator()(u32 i) const { bve_analyze_one(a, i, nullptr); } };
+struct FBveAnalyzeStaged { BveArgs a; HD void operator()(u32 i) const { k_bve_analyze(a, i); } };
 struct FBveWrite { BveArgs a; HD void operator()(u32 i) const { k_bve_write(a, i); } };
 struct FBceCount { BceArgs a; HD void operator()(u32 i) const { k_bce_count(a, i); } };
 struct FBceWrite { BceArgs a; HD void operator()(u32 i) const { k_bce_write(a, i); } };
@@ -65,6 +66,23 @@ struct FEre { EreArgs a; HD void operator()(u32 i) const { k_ere_pv(a, i); } };
 struct FEreResolve { EreArgs a; HD void operator()(u32 i) const { k_ere_resolve(a, i); } };
 struct FEreFix { EreArgs a; const u64* keys; u32 n; HD void operator()() const { ere_fixup(a, keys, n); } };
 struct FEreSeq { EreArgs a; HD void operator()() const { ere_sequential(a); } };
+// Item i of a permuted launch runs f(perm[i]).
+template <class F>
+struct Perm {
+    F f;
+    const u32* perm;
+    HD void operator()(u32 i) const { f(perm[i]); }
+};
+// Work-order key of elected variable k: descending clause count.
+struct FPvKey {
+    Ctx c; const u32* pvs; u32* key; u32* val;
+    HD void operator()(u32 k) const {
+        const u32 p = V2L(pvs[k]);
+        key[k] = 0xFFFFFFFFu - (c.ot_size[p] + c.ot_size[p + 1]);
+        val[k] = k;
+    }
+};
+
 enum Stage { ST_OT = 0, ST_PROP, ST_LCVE, ST_SORT, ST_SUB, ST_VE, ST_BCE, ST_ERE, ST_GC, ST_COUNT, ST_UP, ST_DOWN };
 
 }  // namespace
@@ -95,6 +113,7 @@ struct pf_sigma_ctx {
     DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
     DBuf<uint8_t> mis_state;
     DBuf<u32> mis_big_a, mis_big_b;
+    DBuf<u32> pv_perm, pv_key;
     DBuf<u32> work, cl_stamp;
     DBuf<u32> radix_hist, radix_hscan, scan_tmp32;
     DBuf<u64> scan_tmp64;
@@ -123,6 +142,7 @@ struct pf_sigma_ctx {
     std::vector<uint32_t> dump;
     u64 alg_bytes = 0;
     u32 mis_rounds = 0;
+    bool bve_staged = false;  // BVE decision on shared-memory copies (else straight from HBM)
 
     Ctx view() {
         Ctx c;
@@ -399,6 +419,21 @@ struct pf_sigma_ctx {
         rt.zero(counters64.p + 1, 8);
         SortArgs a{view(), pvs.p, counters64.p + 1};
         rt.each(FSortList{a}, 2 * npvs);
+        // work order of the per-variable kernels: most clauses first (longest
+        // processing time first), so similar variables share a warp and the longest
+        // ones do not start last. Results still go to each variable's elected rank.
+        pv_perm.reserve(rt, nvars + 1);
+        pv_key.reserve(rt, nvars + 1);
+        rt.each(FPvKey{view(), pvs.p, pv_key.p, pv_perm.p}, npvs);
+        radix_sort_pairs(pv_key.p, pv_perm.p, order_k2.p, order_v2.p, npvs, 32, radix_hist.p, radix_hscan.p,
+                         scan_tmp32.p, rt.stream);
+        rt.launches += 20;
+    }
+
+    // f(k) for every elected variable, in work order, dynamically scheduled.
+    template <class F>
+    void pv_each(const F& f) {
+        rt.each_dyn(Perm<F>{f, pv_perm.p}, npvs, counters.p + 11);
     }
 
     // working set of the elected lists, accumulated by the sort kernel
@@ -421,7 +456,7 @@ struct pf_sigma_ctx {
         write_u32(counters.p + 5, 0);
         rt.each(FSubPossible{a, counters.p + 5}, npvs);
         if (read_u32(counters.p + 5) == 0) {
-            rt.each(FSubPv{a}, npvs);
+            pv_each(FSubPv{a});
             check();
             return;
         }
@@ -449,7 +484,7 @@ struct pf_sigma_ctx {
         a.units = sub_units.p;
         a.cap_units = (u32)sub_units.n;
         write_u32(counters.p + 4, 0);
-        rt.each(FSubPv{a}, npvs);
+        pv_each(FSubPv{a});
         check();
         u32 nu = read_u32(counters.p + 4);
         if (nu == 0) return;
@@ -523,7 +558,7 @@ struct pf_sigma_ctx {
             b.pre_lits = sub_pre_lits.p;
             b.run = sub_run.p;
             write_u32(counters.p + 4, 0);
-            rt.each(FSubPv{b}, npvs);
+            pv_each(FSubPv{b});
             check();
             const u32 nn = read_u32(counters.p + 4);
             std::vector<U2> fresh = fetch(sub_units.p, nn);
@@ -586,22 +621,23 @@ struct pf_sigma_ctx {
         a.scr_off = ve_scr_off.p;
         a.scr = ve_scr.p;
 #if SIGMA_CUDA
-        {
+        if (bve_staged) {
             const int smem = kBveThreads * (int)PV_SLOT * 4;
             static bool attr_set = false;
             if (!attr_set) {
                 ck(cudaFuncSetAttribute(bve_analyze_k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "smem attr");
                 attr_set = true;
             }
-            u32 blocks = (npvs + kBveThreads - 1) / kBveThreads;
-            const u32 cap = (u32)rt.sms * 3u;
-            if (blocks > cap) blocks = cap;
+            ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
             rt.launches++;
-            bve_analyze_k<<<blocks, kBveThreads, smem, rt.stream>>>(a);
+            bve_analyze_k<<<(u32)rt.sms * 3u, kBveThreads, smem, rt.stream>>>(a, pv_perm.p, counters.p + 11);
             ck(cudaGetLastError(), "launch");
+        } else {
+            pv_each(FBveAnalyze{a});
         }
 #else
-        rt.each(FBveAnalyze{a}, npvs);
+        if (bve_staged) pv_each(FBveAnalyzeStaged{a});
+        else pv_each(FBveAnalyze{a});
 #endif
         check();
         const u32 add_cls = scan32(ve_ncls.p, ve_cls_scan.p, npvs);
@@ -617,7 +653,7 @@ struct pf_sigma_ctx {
         a.cls_base = ncls;
         a.lit_base = nlits_used;
         a.wit_base = nresolved;
-        rt.each(FBveWrite{a}, npvs);
+        pv_each(FBveWrite{a});
         ncls += add_cls;
         nlits_used += add_lits;
         nresolved += add_wit;
@@ -636,14 +672,14 @@ struct pf_sigma_ctx {
         ve_nwit.reserve(rt, npvs);
         ve_wit_scan.reserve(rt, npvs);
         a.nwit = ve_nwit.p;
-        rt.each(FBceCount{a}, npvs);
+        pv_each(FBceCount{a});
         const u64 add = scan64(ve_nwit.p, ve_wit_scan.p, npvs);
         if (!add) return;
         ensure_resolved(nresolved + add);
         a.c = view();
         a.wit_scan = ve_wit_scan.p;
         a.wit_base = nresolved;
-        rt.each(FBceWrite{a}, npvs);
+        pv_each(FBceWrite{a});
         nresolved += add;
         alg_bytes += 4ull * add;
     }
@@ -678,7 +714,7 @@ struct pf_sigma_ctx {
         a.nlosers = counters.p + 8;
         write_u32(counters.p + 7, 0);
         write_u32(counters.p + 8, 0);
-        rt.each(FEre{a}, npvs);
+        pv_each(FEre{a});
         check();
         const u32 nrec = read_u32(counters.p + 7);
         rt.each(FEreResolve{a}, nrec);
@@ -861,6 +897,7 @@ pf_status pf_sigma_create(const pf_options* opts, pf_sigma_ctx** out) {
         }
         c->rt.init();
         c->tm.init();
+        if (const char* e = std::getenv("SIGMA_BVE_STAGED")) c->bve_staged = e[0] == '1';
         c->counters.reserve(c->rt, 32);
         c->counters64.reserve(c->rt, 8);
         c->rt.zero(c->counters.p, 32 * 4);
@@ -1213,6 +1250,8 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.mis_state, &c.ve_type, &c.sub_run};
     c.mis_big_a.free();
     c.mis_big_b.free();
+    c.pv_perm.free();
+    c.pv_key.free();
     for (auto* b : b8) b->free();
     c.sub_units.free();
     c.sub_pairs.free();
