@@ -124,6 +124,120 @@ HD u32 warp_append(u32* counter, bool pred) {
 #endif
 }
 
+// ---------------------------------------------------------------- warp steps
+// Warp-cooperative code is written as uniform steps whose per-lane parts are
+// lambdas of the lane (or item) index. On the GPU every lane of the warp runs the
+// same step; the serial emulation runs the step once, evaluating the lambda for each
+// lane in turn, so the same source is checked on the CPU.
+constexpr u32 kFull = 0xffffffffu;
+
+HD u32 lane_id() {
+#if defined(__CUDA_ARCH__)
+    return threadIdx.x & 31u;
+#else
+    return 0;
+#endif
+}
+HD void wsync() {
+#if defined(__CUDA_ARCH__)
+    __syncwarp();
+#endif
+}
+// f(i) for i in [0, n), items strided over the lanes; ends with a warp barrier.
+template <class F>
+HD void wfor(u32 n, F f) {
+#if defined(__CUDA_ARCH__)
+    for (u32 i = threadIdx.x & 31u; i < n; i += 32) f(i);
+    __syncwarp();
+#else
+    for (u32 i = 0; i < n; i++) f(i);
+#endif
+}
+// Bit l set when p(l) holds, for lanes l < 32.
+template <class P>
+HD u32 wballot(P p) {
+#if defined(__CUDA_ARCH__)
+    return __ballot_sync(kFull, p(threadIdx.x & 31u));
+#else
+    u32 m = 0;
+    for (u32 l = 0; l < 32; l++) if (p(l)) m |= 1u << l;
+    return m;
+#endif
+}
+// Sum of f(i) over i in [0, n).
+template <class F>
+HD u32 wsum(u32 n, F f) {
+#if defined(__CUDA_ARCH__)
+    u32 s = 0;
+    for (u32 i = threadIdx.x & 31u; i < n; i += 32) s += f(i);
+    return __reduce_add_sync(kFull, s);
+#else
+    u32 s = 0;
+    for (u32 i = 0; i < n; i++) s += f(i);
+    return s;
+#endif
+}
+template <class F>
+HD u64 wsum64(u32 n, F f) {
+#if defined(__CUDA_ARCH__)
+    u64 s = 0;
+    for (u32 i = threadIdx.x & 31u; i < n; i += 32) s += f(i);
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
+    return s;
+#else
+    u64 s = 0;
+    for (u32 i = 0; i < n; i++) s += f(i);
+    return s;
+#endif
+}
+// Smallest i in [0, n) with p(i), or NONE_IDX. p is evaluated on batches of 32 in
+// order and stops at the first batch with a hit.
+constexpr u32 NONE_IDX = 0xFFFFFFFFu;
+template <class P>
+HD u32 wfirst(u32 n, P p) {
+    for (u32 base = 0; base < n; base += 32) {
+        const u32 m = wballot([&](u32 l) { return base + l < n && p(base + l); });
+#if defined(__CUDA_ARCH__)
+        if (m) return base + (u32)(__ffs(m) - 1);
+#else
+        if (m) return base + (u32)__builtin_ctz(m);
+#endif
+    }
+    return NONE_IDX;
+}
+// Minimum of f(i) over i in [0, n) (f returns NONE_IDX for "no value").
+template <class F>
+HD u32 wmin(u32 n, F f) {
+#if defined(__CUDA_ARCH__)
+    u32 m = NONE_IDX;
+    for (u32 i = threadIdx.x & 31u; i < n; i += 32) { const u32 x = f(i); if (x < m) m = x; }
+    return __reduce_min_sync(kFull, m);
+#else
+    u32 m = NONE_IDX;
+    for (u32 i = 0; i < n; i++) { const u32 x = f(i); if (x < m) m = x; }
+    return m;
+#endif
+}
+// Runs f once per warp (lane 0), then a warp barrier.
+template <class F>
+HD void wone(F f) {
+#if defined(__CUDA_ARCH__)
+    if ((threadIdx.x & 31u) == 0) f();
+    __syncwarp();
+#else
+    f();
+#endif
+}
+// Value of lane `src`'s v (uniform broadcast; the emulation's v is already uniform).
+HD u32 wbcast(u32 v, u32 src) {
+#if defined(__CUDA_ARCH__)
+    return __shfl_sync(kFull, v, (int)src);
+#else
+    (void)src;
+    return v;
+#endif
+}
+
 // Volatile load for values that other threads of the same launch may update.
 HD u32 vload(const u32* p) { return *(const volatile u32*)p; }
 

@@ -19,6 +19,7 @@
 #include "cnf.cuh"
 #include "introsort.cuh"
 #include "k_bve_analyze.cuh"
+#include "k_bve_warp.cuh"
 #include "k_sub.cuh"
 
 namespace sigma {
@@ -127,6 +128,59 @@ __global__ void __launch_bounds__(kBveThreads) bve_analyze_k(BveArgs a, const u3
 HD void k_bve_analyze(const BveArgs& a, u32 k) {
     u32 slot[PV_SLOT];
     bve_analyze_one(a, k, slot);
+}
+
+// Step 1 with one warp per elected variable (k_bve_warp.cuh); variables too large
+// for the warp slot take the per-thread decision on lane 0.
+HD void bve_warp_one(const BveArgs& a, u32 k, u32* slot) {
+    VeOpts o;
+    o.ve_clause_max = a.ve_clause_max;
+    o.ve_lbound = a.ve_lbound;
+    o.xor_max_arity = a.xor_max_arity;
+    WarpPv w;
+    w.bind(a.c, slot);
+    VeResult r;
+    const bool staged = wpv_stage(w, a.c, a.pvs[k]);
+    if (staged) r = wpv_bve_decide(w, o);
+    if (lane_id() == 0) {
+        if (!staged) {
+            GlobalPv g;
+            g.init(a.c, a.pvs[k], a.scr + a.scr_off[k]);
+            r = pv_bve_decide(g, o);
+        }
+        a.type[k] = r.type;
+        a.porgs[k] = r.porgs;
+        a.norgs[k] = r.norgs;
+        a.def[k] = r.def;
+        a.ncls[k] = r.ncls;
+        a.nlits[k] = r.nlits;
+        a.nwit[k] = r.nwit;
+    }
+    wsync();
+}
+
+#if SIGMA_CUDA
+constexpr int kBveWarpThreads = 256;
+constexpr u32 kBveWarpChunk = 4;  // variables a warp takes per counter increment
+__global__ void __launch_bounds__(kBveWarpThreads) bve_warp_k(BveArgs a, const u32* perm, u32* next) {
+    extern __shared__ u32 smem[];
+    u32* slot = smem + (threadIdx.x >> 5) * WPV_WORDS;
+    const u32 lane = threadIdx.x & 31u;
+    while (true) {
+        u32 j0 = 0;
+        if (lane == 0) j0 = atomicAdd(next, kBveWarpChunk);
+        j0 = __shfl_sync(0xffffffffu, j0, 0);
+        if (j0 >= a.npvs) break;
+        const u32 j1 = j0 + kBveWarpChunk < a.npvs ? j0 + kBveWarpChunk : a.npvs;
+        for (u32 j = j0; j < j1; j++) bve_warp_one(a, perm[j], slot);
+    }
+}
+#endif
+
+// Emulation entry of the warp path: the slot is a local array, lanes run in turn.
+HD void k_bve_warp(const BveArgs& a, u32 k) {
+    u32 slot[WPV_WORDS];
+    bve_warp_one(a, k, slot);
 }
 
 // ---------------------------------------------------------------- write step

@@ -59,6 +59,7 @@ struct FSubCommit { Ctx c; const u32* lits; HD void operator()(u32 i) const { k_
 struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) const { k_bve_scratch_need(c, pvs, need, i); } };
 struct FBveAnalyze { BveArgs a; HD void operator()(u32 i) const { bve_analyze_one(a, i, nullptr); } };
 struct FBveAnalyzeStaged { BveArgs a; HD void operator()(u32 i) const { k_bve_analyze(a, i); } };
+struct FBveWarp { BveArgs a; HD void operator()(u32 i) const { k_bve_warp(a, i); } };
 struct FBveWrite { BveArgs a; HD void operator()(u32 i) const { k_bve_write(a, i); } };
 struct FBceCount { BceArgs a; HD void operator()(u32 i) const { k_bce_count(a, i); } };
 struct FBceWrite { BceArgs a; HD void operator()(u32 i) const { k_bce_write(a, i); } };
@@ -142,7 +143,7 @@ struct pf_sigma_ctx {
     std::vector<uint32_t> dump;
     u64 alg_bytes = 0;
     u32 mis_rounds = 0;
-    bool bve_staged = false;  // BVE decision on shared-memory copies (else straight from HBM)
+    int bve_mode = 2;  // BVE decision: 0 thread per variable from HBM, 1 thread on a smem copy, 2 warp per variable
 
     Ctx view() {
         Ctx c;
@@ -621,7 +622,18 @@ struct pf_sigma_ctx {
         a.scr_off = ve_scr_off.p;
         a.scr = ve_scr.p;
 #if SIGMA_CUDA
-        if (bve_staged) {
+        if (bve_mode == 2) {
+            const int smem = kBveWarpThreads / 32 * (int)WPV_WORDS * 4;
+            static bool attr_set = false;
+            if (!attr_set) {
+                ck(cudaFuncSetAttribute(bve_warp_k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "smem attr");
+                attr_set = true;
+            }
+            ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
+            rt.launches++;
+            bve_warp_k<<<(u32)rt.sms * 8u, kBveWarpThreads, smem, rt.stream>>>(a, pv_perm.p, counters.p + 11);
+            ck(cudaGetLastError(), "launch");
+        } else if (bve_mode == 1) {
             const int smem = kBveThreads * (int)PV_SLOT * 4;
             static bool attr_set = false;
             if (!attr_set) {
@@ -636,7 +648,8 @@ struct pf_sigma_ctx {
             pv_each(FBveAnalyze{a});
         }
 #else
-        if (bve_staged) pv_each(FBveAnalyzeStaged{a});
+        if (bve_mode == 2) pv_each(FBveWarp{a});
+        else if (bve_mode == 1) pv_each(FBveAnalyzeStaged{a});
         else pv_each(FBveAnalyze{a});
 #endif
         check();
@@ -897,7 +910,7 @@ pf_status pf_sigma_create(const pf_options* opts, pf_sigma_ctx** out) {
         }
         c->rt.init();
         c->tm.init();
-        if (const char* e = std::getenv("SIGMA_BVE_STAGED")) c->bve_staged = e[0] == '1';
+        if (const char* e = std::getenv("SIGMA_BVE_MODE")) c->bve_mode = e[0] - '0';
         c->counters.reserve(c->rt, 32);
         c->counters64.reserve(c->rt, 8);
         c->rt.zero(c->counters.p, 32 * 4);
