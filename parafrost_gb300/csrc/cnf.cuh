@@ -84,6 +84,20 @@ HD int lit_value(const Ctx& c, u32 lit) {
 
 HD void set_err(const Ctx& c, u32 bits) { atom_or(c.err, bits); }
 
+// Header load through the read-only path (for launches that write no header).
+HD Hdr hdr_ro(const Hdr* p) {
+#if defined(__CUDA_ARCH__)
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+    Hdr h;
+    h.start = v.x;
+    h.size = v.y;
+    h.sig = v.z;
+    h.flags = v.w;
+    return h;
+#else
+    return *p;
+#endif
+}
 HD const u32* clause_lits(const Ctx& c, const Hdr& h) { return c.lits + h.start; }
 
 // Signature of a literal array.

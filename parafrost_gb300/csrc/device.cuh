@@ -240,6 +240,15 @@ HD u32 wbcast(u32 v, u32 src) {
 
 // Volatile load for values that other threads of the same launch may update.
 HD u32 vload(const u32* p) { return *(const volatile u32*)p; }
+// Load through the read-only path, for data no thread writes during the launch.
+template <class T>
+HD T ldro(const T* p) {
+#if defined(__CUDA_ARCH__)
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
 
 HD int popc32(u32 x) {
 #if defined(__CUDA_ARCH__)

@@ -9,16 +9,16 @@
 // the co-occurrence graph restricted to F, in rank order, cut at the break
 // candidate B = the first valid candidate that is either outside F (it is never
 // frozen and its lists are necessarily long) or an independent-set member whose
-// lists reach the temperatures. The independent set is decided in parallel
-// rounds: a vertex joins when every lower-ranked neighbour is out, leaves when
-// one lower-ranked neighbour is in (Blelloch-Fineman-Shun deterministic greedy MIS).
+// lists reach the temperatures. The independent set is the greedy one in rank
+// order (a vertex joins when every lower-ranked neighbour is out, leaves when one
+// lower-ranked neighbour is in), decided by frontier waves over the graph.
 #pragma once
 
 #include "cnf.cuh"
 
 namespace sigma {
 
-enum : uint8_t { MIS_NONE = 0, MIS_UNDECIDED = 1, MIS_IN = 2, MIS_OUT = 3 };
+enum : u32 { MIS_NONE = 0, MIS_UNDECIDED = 1, MIS_IN = 2, MIS_OUT = 3 };
 
 struct LcveArgs {
     Ctx c;
@@ -26,9 +26,10 @@ struct LcveArgs {
     u32* score;           // nvars+1
     u32* order;           // nvars: variables in (score, var) order
     u32* rank;            // nvars+1
-    uint8_t* state;       // nvars+1
+    u32* state;           // nvars+1: MIS_* membership of the independent-set graph
+    u32* cnt;             // nvars+1: undecided lower-neighbour occurrences
+    u32* grank;           // nvars+1: rank of a graph vertex, NONE outside the graph
     u32* bound;           // [0] = B0 (first valid non-F rank), [1] = B
-    u32* changed;         // round counter of undecided vertices
     u32* pvs;             // elected variables in rank order
 };
 
@@ -55,128 +56,300 @@ HD void k_rank(const LcveArgs& a, u32 p) {
     if (lcve_valid(a.c, v) && !lcve_freezable(a, v)) atom_min(&a.bound[0], p);
 }
 
-// Work lists of undecided vertices and, per vertex, where its last scan met the first
-// undecided lower neighbour (side:1 | list index:23 | literal index:8). Everything
-// before that point was out or irrelevant, and "out" is final, so the next round
-// resumes there. Indices are capped, which only makes a scan start earlier.
-struct MisList {
-    u32* resume;
-    u32* in;
-    u32* out;
-    u32* nout;
-};
-
-HD u32 mis_pos(u32 side, u32 i, u32 k) {
-    if (i >= 0x7FFFFFu) return (side << 31) | (0x7FFFFFu << 8);  // restart that clause from its first literal
-    return (side << 31) | (i << 8) | (k < 255u ? k : 255u);
-}
-
-// Vertices whose two lists hold more than this many clauses are scanned by a whole
-// warp (one clause per lane) instead of one thread.
+// The independent set is decided by pushing decisions along edges to higher ranks:
+// every graph vertex counts the occurrences of lower-ranked graph neighbours in its
+// live clauses; a vertex with none is in. A vertex that goes in sends every higher
+// neighbour out; a vertex that goes out decrements its higher neighbours' counts, and
+// a count reaching zero means every lower neighbour is out, so that vertex goes in.
+// Each wave processes only the vertices decided in the previous one. A neighbour
+// shared through several clauses is counted and decremented once per clause.
+// Vertices with more than MIS_WARP_MIN_OCC clauses are handled by a whole warp.
 constexpr u32 MIS_WARP_MIN_OCC = 12;
 
-HD void k_mis_init(const LcveArgs& a, const MisList& small, const MisList& big, u32 v) {
-    if (v == 0) { a.state[0] = MIS_NONE; return; }
+struct MisFront {
+    u32* small;   // next frontier, small adjacency
+    u32* nsmall;
+    u32* big;     // next frontier, large adjacency
+    u32* nbig;
+};
+
+HD bool mis_is_big(const Ctx& c, u32 v) { return c.ot_size[V2L(v)] + c.ot_size[NEG(V2L(v))] > MIS_WARP_MIN_OCC; }
+
+HD void mis_append(const MisFront& f, const Ctx& c, u32 v, bool pred) {
+    const bool big = pred && mis_is_big(c, v);
+    const u32 ps = warp_append(f.nsmall, pred && !big);
+    const u32 pb = warp_append(f.nbig, big);
+    if (pred && !big) f.small[ps] = v;
+    if (big) f.big[pb] = v;
+}
+
+// Graph membership (state, grank), and the list of large graph vertices for the warp
+// count.
+HD void k_mis_init(const LcveArgs& a, const MisFront& bigs, u32 v) {
+    if (v == 0) { a.state[0] = MIS_NONE; a.grank[0] = NONE; return; }
     const bool in_graph = lcve_valid(a.c, v) && lcve_freezable(a, v) && a.rank[v] < a.bound[0];
     a.state[v] = in_graph ? MIS_UNDECIDED : MIS_NONE;
-    if (in_graph) small.resume[v] = 0;
-    const bool is_big = in_graph && a.c.ot_size[V2L(v)] + a.c.ot_size[NEG(V2L(v))] > MIS_WARP_MIN_OCC;
-    const u32 ps = warp_append(small.nout, in_graph && !is_big);
-    const u32 pb = warp_append(big.nout, is_big);
-    if (in_graph && !is_big) small.out[ps] = v;
-    if (is_big) big.out[pb] = v;
+    a.grank[v] = in_graph ? a.rank[v] : NONE;
+    const bool big = in_graph && mis_is_big(a.c, v);
+    const u32 pb = warp_append(bigs.nbig, big);
+    if (big) bigs.big[pb] = v;
 }
 
-// One round for an undecided vertex: scan its live clauses from the resume point.
-HD void k_mis_round(const LcveArgs& a, const MisList& w, u32 idx) {
-    const u32 v = w.in[idx];
-    volatile uint8_t* st = (volatile uint8_t*)a.state;
-    if (st[v] != MIS_UNDECIDED) return;
-    const Ctx& c = a.c;
+// The clause walks read literals four at a time, so the loads (and the pushes'
+// atomics) of a chunk are in flight together. Graph ranks, clauses and lists are
+// not written while the independent set is decided.
+constexpr u32 MIS_CHUNK = 4;
+
+// Occurrences of graph vertices ranked below rv (other than v) in live clause r.
+HD u32 mis_lower_in_clause(const LcveArgs& a, u32 v, u32 rv, u32 r) {
+    const Hdr h = hdr_ro(&a.c.hdr[r]);
+    if (h_deleted(h.flags)) return 0;
+    const u32* L = a.c.lits + h.start;
+    u32 n = 0;
+    for (u32 k0 = 0; k0 < h.size; k0 += MIS_CHUNK) {
+        u32 w[MIS_CHUNK];
+#pragma unroll
+        for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < h.size ? ABS(ldro(L + k0 + j)) : v;
+#pragma unroll
+        for (u32 j = 0; j < MIS_CHUNK; j++) n += (w[j] != v && ldro(&a.grank[w[j]]) < rv) ? 1u : 0u;
+    }
+    return n;
+}
+
+// Lower-neighbour count of graph vertex v; a vertex with none goes in and is
+// returned true (the caller puts it on the first frontier).
+HD bool mis_count_one(const LcveArgs& a, u32 v) {
     const u32 rv = a.rank[v];
-    const u32 pos = w.resume[v];
-    const u32 side0 = pos >> 31, i0 = (pos >> 8) & 0x7FFFFFu, k0 = pos & 0xFFu;
-    u32 first = NONE;
-    for (u32 side = side0; side < 2; side++) {
-        const u32 l = V2L(v) + side;
-        const u32 o = c.ot_off[l], s = c.ot_size[l];
-        for (u32 i = side == side0 ? i0 : 0u; i < s; i++) {
-            const Hdr h = c.hdr[c.ot_refs[o + i]];
-            if (h_deleted(h.flags)) continue;
-            const u32* lits = c.lits + h.start;
-            const u32 kstart = (side == side0 && i == i0) ? k0 : 0u;
-            for (u32 k = kstart; k < h.size; k++) {
-                const u32 u = ABS(lits[k]);
-                if (u == v) continue;
-                const uint8_t su = st[u];
-                if (su == MIS_NONE || a.rank[u] > rv) continue;
-                if (su == MIS_IN) { st[v] = MIS_OUT; return; }
-                if (su == MIS_UNDECIDED && first == NONE) first = mis_pos(side, i, k);
-            }
-        }
+    u32 n = 0;
+    for (u32 side = 0; side < 2; side++) {
+        const u32 l = V2L(v) + side, o = a.c.ot_off[l], s = a.c.ot_size[l];
+        for (u32 i = 0; i < s; i++) n += mis_lower_in_clause(a, v, rv, ldro(&a.c.ot_refs[o + i]));
     }
-    if (first == NONE) {
-        st[v] = MIS_IN;
-    } else {
-        w.resume[v] = first;
-        w.out[warp_append(w.nout, true)] = v;
+    a.cnt[v] = n;
+    if (n) return false;
+    a.state[v] = MIS_IN;
+    return true;
+}
+
+// Count for the small graph vertices (the large ones go through the warp kernel).
+HD void k_mis_count(const LcveArgs& a, const MisFront& f, u32 v) {
+    const bool in0 = v && a.state[v] == MIS_UNDECIDED && !mis_is_big(a.c, v) && mis_count_one(a, v);
+    mis_append(f, a.c, v, in0);
+}
+
+// Frontier vertex u (rank ru, in or out) pushes its decision to its higher
+// neighbours in clause r; app(w) is called for each neighbour w this decides. An
+// out vertex decrements unconditionally: a decided neighbour's count no longer
+// matters, and a neighbour that is in never receives a decrement (its count reached
+// zero only after every lower neighbour's).
+template <class App>
+HD void mis_push_one(const LcveArgs& a, u32 u, u32 ru, bool in, u32 r, App app) {
+    const Hdr h = hdr_ro(&a.c.hdr[r]);
+    if (h_deleted(h.flags)) return;
+    const u32* L = a.c.lits + h.start;
+    for (u32 k0 = 0; k0 < h.size; k0 += MIS_CHUNK) {
+        u32 w[MIS_CHUNK], old[MIS_CHUNK];
+        bool up[MIS_CHUNK];
+#pragma unroll
+        for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < h.size ? ABS(ldro(L + k0 + j)) : u;
+#pragma unroll
+        for (u32 j = 0; j < MIS_CHUNK; j++) {
+            const u32 g = w[j] != u ? ldro(&a.grank[w[j]]) : NONE;
+            up[j] = g != NONE && g > ru;
+        }
+#pragma unroll
+        for (u32 j = 0; j < MIS_CHUNK; j++)
+            if (up[j]) old[j] = in ? atom_cas(&a.state[w[j]], MIS_UNDECIDED, MIS_OUT) : atom_add(&a.cnt[w[j]], 0xFFFFFFFFu);
+#pragma unroll
+        for (u32 j = 0; j < MIS_CHUNK; j++) {
+            if (!up[j]) continue;
+            const bool dec = in ? old[j] == MIS_UNDECIDED
+                                : (old[j] == 1u && atom_cas(&a.state[w[j]], MIS_UNDECIDED, MIS_IN) == MIS_UNDECIDED);
+            if (dec) app(w[j]);
+        }
     }
 }
 
-#if SIGMA_CUDA
-// The same round with one warp per vertex: lanes take consecutive clauses of the
-// two lists (from the resume point, at clause granularity), ballots give "some lower
-// neighbour is in" and the first clause holding an undecided lower neighbour.
-__global__ void mis_round_warp_k(LcveArgs a, MisList w, u32 n) {
-    const u32 lane = threadIdx.x & 31u;
-    const u32 nwarps = (gridDim.x * blockDim.x) >> 5;
-    volatile uint8_t* st = (volatile uint8_t*)a.state;
-    const Ctx& c = a.c;
-    for (u32 idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < n; idx += nwarps) {
-        const u32 v = w.in[idx];
-        if (st[v] != MIS_UNDECIDED) continue;
+// Frontier vertex u pushes through all its clauses.
+template <class App>
+HD void mis_push_vertex(const LcveArgs& a, u32 u, App app) {
+    const bool in = vload(&a.state[u]) == MIS_IN;
+    const u32 ru = a.rank[u];
+    for (u32 side = 0; side < 2; side++) {
+        const u32 l = V2L(u) + side, o = a.c.ot_off[l], s = a.c.ot_size[l];
+        for (u32 i = 0; i < s; i++) mis_push_one(a, u, ru, in, ldro(&a.c.ot_refs[o + i]), app);
+    }
+}
+
+#if !SIGMA_CUDA
+HD void k_mis_count_big(const LcveArgs& a, const u32* in, const MisFront& f, u32 idx) {
+    const u32 v = in[idx];
+    if (mis_count_one(a, v)) f.big[atom_add(f.nbig, 1u)] = v;
+}
+// One wave step of the serial build: frontier vertex in[idx] pushes, decided
+// vertices go straight to the next lists.
+HD void k_mis_push(const LcveArgs& a, const u32* in, const MisFront& f, u32 idx) {
+    mis_push_vertex(a, in[idx], [&](u32 w) {
+        if (mis_is_big(a.c, w)) f.big[atom_add(f.nbig, 1u)] = w;
+        else f.small[atom_add(f.nsmall, 1u)] = w;
+    });
+}
+#else
+// Count for the large graph vertices, one warp each (lanes take its clauses). The
+// list length is read from device memory (no host round trip).
+__global__ void mis_count_warp_k(LcveArgs a, const u32* in, const u32* n_ptr, MisFront f) {
+    const u32 lane = threadIdx.x & 31u, nw = (gridDim.x * blockDim.x) >> 5;
+    const u32 n = *n_ptr;
+    for (u32 idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < n; idx += nw) {
+        const u32 v = in[idx];
         const u32 rv = a.rank[v];
-        const u32 pos = w.resume[v];
-        const u32 side0 = pos >> 31, i0 = (pos >> 8) & 0x7FFFFFu;
-        const u32 np = c.ot_size[V2L(v)], nn = c.ot_size[NEG(V2L(v))];
-        const u32 op = c.ot_off[V2L(v)], on = c.ot_off[NEG(V2L(v))];
-        const u32 total = np + nn;
-        const u32 t0 = side0 ? np + (i0 < nn ? i0 : nn) : (i0 < np ? i0 : np);
-        u32 first = NONE;
-        bool out = false;
-        for (u32 base = t0; base < total; base += 32) {
-            const u32 t = base + lane;
-            bool has_in = false, has_und = false;
-            if (t < total) {
-                const Hdr h = c.hdr[c.ot_refs[t < np ? op + t : on + (t - np)]];
-                if (!h_deleted(h.flags)) {
-                    const u32* L = c.lits + h.start;
-                    for (u32 k = 0; k < h.size; k++) {
-                        const u32 u = ABS(L[k]);
-                        if (u == v) continue;
-                        const uint8_t su = st[u];
-                        if (su == MIS_NONE || a.rank[u] > rv) continue;
-                        if (su == MIS_IN) { has_in = true; break; }
-                        if (su == MIS_UNDECIDED) has_und = true;
-                    }
-                }
-            }
-            if (__ballot_sync(0xffffffffu, has_in)) { out = true; break; }
-            const u32 und = __ballot_sync(0xffffffffu, has_und);
-            if (und && first == NONE) {
-                const u32 tt = base + (u32)(__ffs(und) - 1);
-                first = tt < np ? mis_pos(0, tt, 0) : mis_pos(1, tt - np, 0);
-            }
-        }
+        const u32 p = V2L(v), np = a.c.ot_size[p], nn = a.c.ot_size[p + 1];
+        const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
+        u32 cnt = 0;
+        for (u32 t = lane; t < np + nn; t += 32)
+            cnt += mis_lower_in_clause(a, v, rv, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)]));
+        cnt = __reduce_add_sync(0xffffffffu, cnt);
         if (lane == 0) {
-            if (out) st[v] = MIS_OUT;
-            else if (first == NONE) st[v] = MIS_IN;
-            else {
-                w.resume[v] = first;
-                w.out[atomicAdd(w.nout, 1u)] = v;
+            a.cnt[v] = cnt;
+            if (cnt == 0) {
+                a.state[v] = MIS_IN;
+                f.big[atomicAdd(f.nbig, 1u)] = v;
             }
         }
         __syncwarp();
+    }
+}
+
+// All frontier waves in one cooperative launch. Wave k reads the lists small[k&1],
+// big[k&1] with lengths in counter pair k%3 and appends to the other lists through
+// pair (k+1)%3; pair (k+2)%3, last read in wave k-1, is cleared for wave k+1. A
+// grid barrier separates the waves.
+struct MisWaves {
+    u32* small[2];
+    u32* big[2];
+    u32* ctr;        // three (small, big) length pairs; pair 0 holds the first frontier
+    u32* bar;        // grid barrier: [0] arrivals, [1] generation
+    u32* waves;      // out: number of waves run
+    u32 max_waves;
+};
+
+constexpr u64 kBarrierNs = 2000000000ull;  // a barrier wait longer than 2 s is an error
+
+DEV u64 global_ns() {
+    u64 t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Barrier over all blocks of a cooperative launch. A block whose wait runs out
+// records ERR_ITER and gets false (the launch then winds down).
+DEV bool grid_barrier(u32* bar, u32* err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const u32 gen = vload(&bar[1]);
+        __threadfence();
+        if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        } else {
+            const u64 t0 = global_ns();
+            while (vload(&bar[1]) == gen) {
+                if (global_ns() - t0 > kBarrierNs) {
+                    atomicOr(err, ERR_ITER);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Vertices decided in a wave are staged per block in shared memory and copied to
+// the next lists with one reservation per block (a vertex that finds its block's
+// queue full goes to the list directly).
+constexpr u32 MIS_QCAP = 2048;
+
+struct MisBlockQueue {
+    u32 small[MIS_QCAP], big[MIS_QCAP];
+    u32 ns, nb, base_s, base_b;
+};
+
+DEV void mis_queue_push(MisBlockQueue& q, const MisFront& f, const Ctx& c, u32 w) {
+    if (mis_is_big(c, w)) {
+        const u32 k = atomicAdd(&q.nb, 1u);
+        if (k < MIS_QCAP) q.big[k] = w;
+        else f.big[atomicAdd(f.nbig, 1u)] = w;
+    } else {
+        const u32 k = atomicAdd(&q.ns, 1u);
+        if (k < MIS_QCAP) q.small[k] = w;
+        else f.small[atomicAdd(f.nsmall, 1u)] = w;
+    }
+}
+
+DEV void mis_queue_flush(MisBlockQueue& q, const MisFront& f) {
+    __syncthreads();
+    const u32 ns = q.ns < MIS_QCAP ? q.ns : MIS_QCAP, nb = q.nb < MIS_QCAP ? q.nb : MIS_QCAP;
+    if (threadIdx.x == 0) {
+        q.base_s = ns ? atomicAdd(f.nsmall, ns) : 0u;
+        q.base_b = nb ? atomicAdd(f.nbig, nb) : 0u;
+    }
+    __syncthreads();
+    for (u32 i = threadIdx.x; i < ns; i += blockDim.x) f.small[q.base_s + i] = q.small[i];
+    for (u32 i = threadIdx.x; i < nb; i += blockDim.x) f.big[q.base_b + i] = q.big[i];
+    __syncthreads();
+    if (threadIdx.x == 0) q.ns = q.nb = 0;
+}
+
+__global__ void __launch_bounds__(256) mis_waves_k(LcveArgs a, MisWaves w) {
+    __shared__ MisBlockQueue q;
+    const u32 tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const u32 lane = threadIdx.x & 31u, nwarps = nth >> 5;
+    if (threadIdx.x == 0) q.ns = q.nb = 0;
+    __syncthreads();
+    for (u32 wave = 0;; wave++) {
+        const u32 cur = wave % 3, nxt = (wave + 1) % 3, old = (wave + 2) % 3;
+        const u32 ns = vload(&w.ctr[2 * cur]), nb = vload(&w.ctr[2 * cur + 1]);
+        if (!ns && !nb) {
+            if (tid == 0) *w.waves = wave;
+            return;
+        }
+        if (wave >= w.max_waves) {
+            if (tid == 0) atomicOr(a.c.err, ERR_ITER);
+            return;
+        }
+        if (tid == 0) {
+            w.ctr[2 * old] = 0;
+            w.ctr[2 * old + 1] = 0;
+        }
+        MisFront f;
+        f.small = w.small[(wave + 1) & 1];
+        f.nsmall = &w.ctr[2 * nxt];
+        f.big = w.big[(wave + 1) & 1];
+        f.nbig = &w.ctr[2 * nxt + 1];
+        const auto app = [&](u32 v) { mis_queue_push(q, f, a.c, v); };
+        // the lists were written in the previous wave by other blocks: read them uncached
+        const u32* in_b = w.big[wave & 1];
+        for (u32 idx = tid >> 5; idx < nb; idx += nwarps) {
+            const u32 u = vload(&in_b[idx]);
+            const bool uin = vload(&a.state[u]) == MIS_IN;
+            const u32 ru = a.rank[u];
+            const u32 p = V2L(u), np = a.c.ot_size[p], nn = a.c.ot_size[p + 1];
+            const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
+            for (u32 t = lane; t < np + nn; t += 32)
+                mis_push_one(a, u, ru, uin, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)]), app);
+            __syncwarp();
+        }
+        const u32* in_s = w.small[wave & 1];
+        for (u32 idx = tid; idx < ns; idx += nth) mis_push_vertex(a, vload(&in_s[idx]), app);
+        mis_queue_flush(q, f);
+        if (!grid_barrier(w.bar, a.c.err)) return;
     }
 }
 #endif

@@ -42,8 +42,12 @@ struct FPropClause { PropArgs a; HD void operator()(u32 i) const { k_prop_clause
 struct FReduce { Ctx c; HD void operator()(u32 i) const { k_reduce_list(c, i); } };
 struct FScores { LcveArgs a; HD void operator()(u32 i) const { k_scores(a, i); } };
 struct FRank { LcveArgs a; HD void operator()(u32 i) const { k_rank(a, i); } };
-struct FMisInit { LcveArgs a; MisList s, b; HD void operator()(u32 i) const { k_mis_init(a, s, b, i); } };
-struct FMisRound { LcveArgs a; MisList w; HD void operator()(u32 i) const { k_mis_round(a, w, i); } };
+struct FMisInit { LcveArgs a; MisFront b; HD void operator()(u32 i) const { k_mis_init(a, b, i); } };
+struct FMisCount { LcveArgs a; MisFront f; HD void operator()(u32 i) const { k_mis_count(a, f, i); } };
+#if !SIGMA_CUDA
+struct FMisPush { LcveArgs a; const u32* in; MisFront f; HD void operator()(u32 i) const { k_mis_push(a, in, f, i); } };
+struct FMisCountBig { LcveArgs a; const u32* in; MisFront f; HD void operator()(u32 i) const { k_mis_count_big(a, in, f, i); } };
+#endif
 struct FMisBound { LcveArgs a; HD void operator()(u32 i) const { k_mis_bound(a, i); } };
 struct FElectFlag { LcveArgs a; u32* flags; HD void operator()(u32 i) const { k_elect_flag(a, flags, i); } };
 struct FElectWrite { LcveArgs a; const u32* flags; const u32* scan; HD void operator()(u32 i) const { k_elect_write(a, flags, scan, i); } };
@@ -112,8 +116,7 @@ struct pf_sigma_ctx {
     DBuf<u64> counters64; // [0] nresolved, [1..] scratch
     // stage scratch
     DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
-    DBuf<uint8_t> mis_state;
-    DBuf<u32> mis_big_a, mis_big_b;
+    DBuf<u32> mis_state, mis_big_a, mis_big_b;
     DBuf<u32> pv_perm, pv_key;
     DBuf<u32> work, cl_stamp;
     DBuf<u32> radix_hist, radix_hscan, scan_tmp32;
@@ -190,6 +193,19 @@ struct pf_sigma_ctx {
         return v;
     }
     void write_u32(u32* d, u32 v) { rt.h2d(d, &v, 4); }
+#if SIGMA_CUDA
+    // Blocks of the cooperative wave kernel: every block must be resident at once.
+    int waves_grid = 0;
+    int mis_waves_grid() {
+        if (!waves_grid) {
+            int per_sm = 0;
+            ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mis_waves_k, 256, 0), "occupancy");
+            if (per_sm < 1) throw std::runtime_error("the wave kernel cannot be resident");
+            waves_grid = per_sm * rt.sms;
+        }
+        return waves_grid;
+    }
+#endif
     void write_u64(u64* d, u64 v) { rt.h2d(d, &v, 8); }
 
     // exclusive scans
@@ -357,8 +373,9 @@ struct pf_sigma_ctx {
         a.order = order.p;
         a.rank = rank.p;
         a.state = mis_state.p;
+        a.cnt = order_v2.p;    // the radix sort's scratch and sorted keys, free after it
+        a.grank = order_k2.p;
         a.bound = bound.p;
-        a.changed = counters.p + 3;
         a.pvs = pvs.p;
         rt.zero(score.p, (size_t)(nvars + 1) * 4);
         rt.each(FScores{a}, nvars + 1);
@@ -370,36 +387,50 @@ struct pf_sigma_ctx {
         u32 init_b[2] = {NONE, NONE};
         rt.h2d(bound.p, init_b, 8);
         rt.each(FRank{a}, nvars);
-        // work lists of undecided vertices, small and large adjacency (ping-pong pairs);
-        // resume points in order_v2 (free after the sort)
+        // Independent set by frontier waves. The frontier lists (small / large
+        // adjacency) alternate between flags|mis_big_a and flags_scan|mis_big_b.
         mis_big_a.reserve(rt, nvars + 1);
         mis_big_b.reserve(rt, nvars + 1);
-        MisList ws{order_v2.p, flags_scan.p, flags.p, counters.p + 3};
-        MisList wb{order_v2.p, mis_big_b.p, mis_big_a.p, counters.p + 10};
-        write_u32(counters.p + 3, 0);
-        write_u32(counters.p + 10, 0);
-        rt.each(FMisInit{a, ws, wb}, nvars + 1);
-        u32 pend_s = read_u32(counters.p + 3), pend_b = read_u32(counters.p + 10), rounds = 0;
-        while (pend_s || pend_b) {
-            if (++rounds > nvars + 2) throw int(PF_ETIMEOUT);
-            // last round's output list is this round's input
-            std::swap(ws.out, ws.in);
-            std::swap(wb.out, wb.in);
-            write_u32(counters.p + 3, 0);
-            write_u32(counters.p + 10, 0);
-            if (pend_s) rt.each(FMisRound{a, ws}, pend_s);
-            if (pend_b) {
+        u32* ctr = counters.p + 12;  // [12..17] frontier lengths, [18..19] barrier, [20] waves
+        rt.zero(ctr, 9 * 4);
+        rt.each(FMisInit{a, MisFront{nullptr, nullptr, mis_big_b.p, ctr + 3}}, nvars + 1);
+        MisFront f0{flags.p, ctr, mis_big_a.p, ctr + 1};
+        rt.each(FMisCount{a, f0}, nvars + 1);
+        u32 rounds = 0;
 #if SIGMA_CUDA
-                rt.launches++;
-                mis_round_warp_k<<<rt.grid(pend_b * 32u, 8), 256, 0, rt.stream>>>(a, wb, pend_b);
-                ck(cudaGetLastError(), "launch");
+        rt.launches += 2;
+        mis_count_warp_k<<<rt.sms * 8, 256, 0, rt.stream>>>(a, mis_big_b.p, ctr + 3, f0);
+        ck(cudaGetLastError(), "launch");
+        MisWaves w;
+        w.small[0] = flags.p;
+        w.small[1] = flags_scan.p;
+        w.big[0] = mis_big_a.p;
+        w.big[1] = mis_big_b.p;
+        w.ctr = ctr;
+        w.bar = ctr + 6;
+        w.waves = ctr + 8;
+        w.max_waves = nvars + 2;
+        rt.zero(ctr + 2, 4 * 4);  // the count-list length in pair 1, and the barrier
+        void* args[] = {&a, &w};
+        ck(cudaLaunchCooperativeKernel((const void*)mis_waves_k, dim3(mis_waves_grid()), dim3(256), args, 0, rt.stream),
+           "cooperative launch");
+        check();
+        rounds = read_u32(ctr + 8);
 #else
-                rt.each(FMisRound{a, wb}, pend_b);
-#endif
-            }
-            pend_s = read_u32(counters.p + 3);
-            pend_b = read_u32(counters.p + 10);
+        rt.each(FMisCountBig{a, mis_big_b.p, f0}, read_u32(ctr + 3));
+        MisFront fin = f0;
+        MisFront fout{flags_scan.p, ctr + 2, mis_big_b.p, ctr + 3};
+        u32 pend[2];
+        rt.d2h(pend, ctr, 8);
+        while (pend[0] || pend[1]) {
+            if (++rounds > nvars + 2) throw int(PF_ETIMEOUT);
+            rt.zero(fout.nsmall, 8);
+            if (pend[0]) rt.each(FMisPush{a, fin.small, fout}, pend[0]);
+            if (pend[1]) rt.each(FMisPush{a, fin.big, fout}, pend[1]);
+            std::swap(fin, fout);
+            rt.d2h(pend, fin.nsmall, 8);
         }
+#endif
         mis_rounds += rounds;
         rt.d2d(bound.p + 1, bound.p, 4);
         rt.each(FMisBound{a}, nvars + 1);
@@ -1260,7 +1291,8 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     DBuf<u64>* b64[] = {&c.counters64, &c.scan_tmp64, &c.big64a, &c.big64b, &c.ve_scr_off, &c.ve_lit_scan,
                         &c.ve_wit_scan, &c.sub_wrd, &c.sub_wrd_off, &c.ere_claim, &c.ere_key};
     for (auto* b : b64) b->free();
-    DBuf<uint8_t>* b8[] = {&c.vstate, &c.mis_state, &c.ve_type, &c.sub_run};
+    DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
+    c.mis_state.free();
     c.mis_big_a.free();
     c.mis_big_b.free();
     c.pv_perm.free();
