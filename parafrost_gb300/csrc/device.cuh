@@ -73,6 +73,13 @@ HD u32 atom_cas(u32* p, u32 cmp, u32 v) {
     u32 o = *p; if (o == cmp) *p = v; return o;
 #endif
 }
+HD u64 atom_or64(u64* p, u64 v) {
+#if defined(__CUDA_ARCH__)
+    return (u64)atomicOr((unsigned long long*)p, (unsigned long long)v);
+#else
+    u64 o = *p; *p = o | v; return o;
+#endif
+}
 HD u32 atom_or(u32* p, u32 v) {
 #if defined(__CUDA_ARCH__)
     return atomicOr(p, v);
@@ -240,6 +247,7 @@ HD u32 wbcast(u32 v, u32 src) {
 
 // Volatile load for values that other threads of the same launch may update.
 HD u32 vload(const u32* p) { return *(const volatile u32*)p; }
+HD u64 vload64(const u64* p) { return *(const volatile u64*)p; }
 // Load through the read-only path, for data no thread writes during the launch.
 template <class T>
 HD T ldro(const T* p) {

@@ -18,7 +18,17 @@
 
 namespace sigma {
 
-enum : u32 { MIS_NONE = 0, MIS_UNDECIDED = 1, MIS_IN = 2, MIS_OUT = 3 };
+// Independent-set word of a variable (one 64-bit word, so a neighbour test and its
+// update touch one sector): bits 0-31 the variable's rank if it is a vertex of the
+// graph (NONE otherwise, which never changes while the set is decided), bits 32-61
+// the count of lower-neighbour occurrences not yet out, bits 62-63 the decision.
+enum : u32 { MIS_UNDECIDED = 0, MIS_IN = 1, MIS_OUT = 2 };
+constexpr u64 MIS_CNT_ONE = 1ull << 32;
+constexpr u32 MIS_CNT_MAX = (1u << 30) - 1u;
+HD u32 mis_rank(u64 w) { return (u32)w; }
+HD u32 mis_cnt(u64 w) { return (u32)(w >> 32) & MIS_CNT_MAX; }
+HD u32 mis_dec(u64 w) { return (u32)(w >> 62); }
+HD u64 mis_dec_bits(u32 d) { return (u64)d << 62; }
 
 struct LcveArgs {
     Ctx c;
@@ -26,9 +36,8 @@ struct LcveArgs {
     u32* score;           // nvars+1
     u32* order;           // nvars: variables in (score, var) order
     u32* rank;            // nvars+1
-    u32* state;           // nvars+1: MIS_* membership of the independent-set graph
-    u32* cnt;             // nvars+1: undecided lower-neighbour occurrences
-    u32* grank;           // nvars+1: rank of a graph vertex, NONE outside the graph
+    u64* word;            // nvars+1: independent-set words
+    u64* ws_bytes;        // accumulates the graph's working set (4*occ + sum(8 + 4*len))
     u32* bound;           // [0] = B0 (first valid non-F rank), [1] = B
     u32* pvs;             // elected variables in rank order
 };
@@ -83,27 +92,26 @@ HD void mis_append(const MisFront& f, const Ctx& c, u32 v, bool pred) {
     if (big) f.big[pb] = v;
 }
 
-// Graph membership (state, grank), and the list of large graph vertices for the warp
-// count.
+// Graph membership, and the list of large graph vertices for the warp count.
 HD void k_mis_init(const LcveArgs& a, const MisFront& bigs, u32 v) {
-    if (v == 0) { a.state[0] = MIS_NONE; a.grank[0] = NONE; return; }
-    const bool in_graph = lcve_valid(a.c, v) && lcve_freezable(a, v) && a.rank[v] < a.bound[0];
-    a.state[v] = in_graph ? MIS_UNDECIDED : MIS_NONE;
-    a.grank[v] = in_graph ? a.rank[v] : NONE;
+    const bool in_graph = v && lcve_valid(a.c, v) && lcve_freezable(a, v) && a.rank[v] < a.bound[0];
+    a.word[v] = in_graph ? a.rank[v] : NONE;
     const bool big = in_graph && mis_is_big(a.c, v);
     const u32 pb = warp_append(bigs.nbig, big);
     if (big) bigs.big[pb] = v;
 }
 
 // The clause walks read literals four at a time, so the loads (and the pushes'
-// atomics) of a chunk are in flight together. Graph ranks, clauses and lists are
-// not written while the independent set is decided.
+// atomics) of a chunk are in flight together. Clauses and lists are not written
+// while the independent set is decided.
 constexpr u32 MIS_CHUNK = 4;
 
-// Occurrences of graph vertices ranked below rv (other than v) in live clause r.
-HD u32 mis_lower_in_clause(const LcveArgs& a, u32 v, u32 rv, u32 r) {
+// Occurrences of graph vertices ranked below rv (other than v) in clause r, and
+// the clause's bytes (8 + 4*len when live) added to ws.
+HD u32 mis_lower_in_clause(const LcveArgs& a, u32 v, u32 rv, u32 r, u64& ws) {
     const Hdr h = hdr_ro(&a.c.hdr[r]);
     if (h_deleted(h.flags)) return 0;
+    ws += 8ull + 4ull * h.size;
     const u32* L = a.c.lits + h.start;
     u32 n = 0;
     for (u32 k0 = 0; k0 < h.size; k0 += MIS_CHUNK) {
@@ -111,80 +119,104 @@ HD u32 mis_lower_in_clause(const LcveArgs& a, u32 v, u32 rv, u32 r) {
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < h.size ? ABS(ldro(L + k0 + j)) : v;
 #pragma unroll
-        for (u32 j = 0; j < MIS_CHUNK; j++) n += (w[j] != v && ldro(&a.grank[w[j]]) < rv) ? 1u : 0u;
+        for (u32 j = 0; j < MIS_CHUNK; j++) n += (w[j] != v && mis_rank(a.word[w[j]]) < rv) ? 1u : 0u;
     }
     return n;
 }
 
-// Lower-neighbour count of graph vertex v; a vertex with none goes in and is
-// returned true (the caller puts it on the first frontier).
-HD bool mis_count_one(const LcveArgs& a, u32 v) {
-    const u32 rv = a.rank[v];
+// Stores the lower-neighbour count of graph vertex v; a vertex with none goes in
+// and is returned true (the caller puts it on the first frontier).
+HD bool mis_set_count(const LcveArgs& a, u32 v, u32 rv, u32 n) {
+    if (n > MIS_CNT_MAX) {  // cannot be held: stop the election with an error
+        atom_or(a.c.err, ERR_CAP_SCRATCH);
+        n = MIS_CNT_MAX;
+    }
+    a.word[v] = (u64)rv | ((u64)n << 32) | (n ? 0ull : mis_dec_bits(MIS_IN));
+    return n == 0;
+}
+
+HD bool mis_count_one(const LcveArgs& a, u32 v, u64& ws) {
+    const u32 rv = mis_rank(a.word[v]);
     u32 n = 0;
     for (u32 side = 0; side < 2; side++) {
         const u32 l = V2L(v) + side, o = a.c.ot_off[l], s = a.c.ot_size[l];
-        for (u32 i = 0; i < s; i++) n += mis_lower_in_clause(a, v, rv, ldro(&a.c.ot_refs[o + i]));
+        ws += 4ull * s;
+        for (u32 i = 0; i < s; i++) n += mis_lower_in_clause(a, v, rv, ldro(&a.c.ot_refs[o + i]), ws);
     }
-    a.cnt[v] = n;
-    if (n) return false;
-    a.state[v] = MIS_IN;
-    return true;
+    return mis_set_count(a, v, rv, n);
 }
 
 // Count for the small graph vertices (the large ones go through the warp kernel).
 HD void k_mis_count(const LcveArgs& a, const MisFront& f, u32 v) {
-    const bool in0 = v && a.state[v] == MIS_UNDECIDED && !mis_is_big(a.c, v) && mis_count_one(a, v);
+    u64 ws = 0;
+    const bool in0 = v && mis_rank(a.word[v]) != NONE && !mis_is_big(a.c, v) && mis_count_one(a, v, ws);
     mis_append(f, a.c, v, in0);
+    warp_sum_add64(a.ws_bytes, ws);
 }
 
 // Frontier vertex u (rank ru, in or out) pushes its decision to its higher
 // neighbours in clause r; app(w) is called for each neighbour w this decides. An
-// out vertex decrements unconditionally: a decided neighbour's count no longer
-// matters, and a neighbour that is in never receives a decrement (its count reached
-// zero only after every lower neighbour's).
+// in vertex marks them out; an out vertex decrements their counts unconditionally
+// (a decided neighbour's count no longer matters; a count cannot fall below the
+// occurrences of a lower neighbour that is in, which never decrements), and the
+// push that takes a count from one to zero marks that neighbour in: no other push
+// can reach it any more.
 template <class App>
-HD void mis_push_one(const LcveArgs& a, u32 u, u32 ru, bool in, u32 r, App app) {
-    const Hdr h = hdr_ro(&a.c.hdr[r]);
+HD void mis_push_clause(const LcveArgs& a, u32 u, u32 ru, bool in, const Hdr& h, App app) {
     if (h_deleted(h.flags)) return;
     const u32* L = a.c.lits + h.start;
     for (u32 k0 = 0; k0 < h.size; k0 += MIS_CHUNK) {
-        u32 w[MIS_CHUNK], old[MIS_CHUNK];
+        u32 w[MIS_CHUNK];
+        u64 old[MIS_CHUNK];
         bool up[MIS_CHUNK];
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < h.size ? ABS(ldro(L + k0 + j)) : u;
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) {
-            const u32 g = w[j] != u ? ldro(&a.grank[w[j]]) : NONE;
+            const u32 g = w[j] != u ? mis_rank(a.word[w[j]]) : NONE;
             up[j] = g != NONE && g > ru;
         }
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++)
-            if (up[j]) old[j] = in ? atom_cas(&a.state[w[j]], MIS_UNDECIDED, MIS_OUT) : atom_add(&a.cnt[w[j]], 0xFFFFFFFFu);
+            if (up[j]) old[j] = in ? atom_or64(&a.word[w[j]], mis_dec_bits(MIS_OUT)) : atom_add64(&a.word[w[j]], 0ull - MIS_CNT_ONE);
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) {
-            if (!up[j]) continue;
-            const bool dec = in ? old[j] == MIS_UNDECIDED
-                                : (old[j] == 1u && atom_cas(&a.state[w[j]], MIS_UNDECIDED, MIS_IN) == MIS_UNDECIDED);
-            if (dec) app(w[j]);
+            if (!up[j] || mis_dec(old[j]) != MIS_UNDECIDED) continue;
+            if (in) {
+                app(w[j]);
+            } else if (mis_cnt(old[j]) == 1u) {
+                atom_or64(&a.word[w[j]], mis_dec_bits(MIS_IN));
+                app(w[j]);
+            }
         }
     }
 }
 
-// Frontier vertex u pushes through all its clauses.
+// Frontier vertex u pushes through all its clauses. The next clause's header is
+// loaded before the current clause's atomics, so two clause walks overlap.
 template <class App>
 HD void mis_push_vertex(const LcveArgs& a, u32 u, App app) {
-    const bool in = vload(&a.state[u]) == MIS_IN;
-    const u32 ru = a.rank[u];
-    for (u32 side = 0; side < 2; side++) {
-        const u32 l = V2L(u) + side, o = a.c.ot_off[l], s = a.c.ot_size[l];
-        for (u32 i = 0; i < s; i++) mis_push_one(a, u, ru, in, ldro(&a.c.ot_refs[o + i]), app);
+    const u64 wu = vload64(&a.word[u]);
+    const bool in = mis_dec(wu) == MIS_IN;
+    const u32 ru = mis_rank(wu);
+    const u32 p = V2L(u), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
+    const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
+    if (!n) return;
+    Hdr h = hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[op])]);
+    for (u32 t = 0; t < n; t++) {
+        Hdr hn = h;
+        if (t + 1 < n) hn = hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1])]);
+        mis_push_clause(a, u, ru, in, h, app);
+        h = hn;
     }
 }
 
 #if !SIGMA_CUDA
 HD void k_mis_count_big(const LcveArgs& a, const u32* in, const MisFront& f, u32 idx) {
     const u32 v = in[idx];
-    if (mis_count_one(a, v)) f.big[atom_add(f.nbig, 1u)] = v;
+    u64 ws = 0;
+    if (mis_count_one(a, v, ws)) f.big[atom_add(f.nbig, 1u)] = v;
+    *a.ws_bytes += ws;
 }
 // One wave step of the serial build: frontier vertex in[idx] pushes, decided
 // vertices go straight to the next lists.
@@ -202,19 +234,18 @@ __global__ void mis_count_warp_k(LcveArgs a, const u32* in, const u32* n_ptr, Mi
     const u32 n = *n_ptr;
     for (u32 idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < n; idx += nw) {
         const u32 v = in[idx];
-        const u32 rv = a.rank[v];
+        const u32 rv = mis_rank(a.word[v]);
         const u32 p = V2L(v), np = a.c.ot_size[p], nn = a.c.ot_size[p + 1];
         const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
         u32 cnt = 0;
+        u64 ws = 0;
         for (u32 t = lane; t < np + nn; t += 32)
-            cnt += mis_lower_in_clause(a, v, rv, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)]));
+            cnt += mis_lower_in_clause(a, v, rv, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)]), ws);
         cnt = __reduce_add_sync(0xffffffffu, cnt);
+        for (int o = 16; o; o >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, o);
         if (lane == 0) {
-            a.cnt[v] = cnt;
-            if (cnt == 0) {
-                a.state[v] = MIS_IN;
-                f.big[atomicAdd(f.nbig, 1u)] = v;
-            }
+            atomicAdd((unsigned long long*)a.ws_bytes, (unsigned long long)(ws + 4ull * (np + nn)));
+            if (mis_set_count(a, v, rv, cnt)) f.big[atomicAdd(f.nbig, 1u)] = v;
         }
         __syncwarp();
     }
@@ -338,12 +369,13 @@ __global__ void __launch_bounds__(256) mis_waves_k(LcveArgs a, MisWaves w) {
         const u32* in_b = w.big[wave & 1];
         for (u32 idx = tid >> 5; idx < nb; idx += nwarps) {
             const u32 u = vload(&in_b[idx]);
-            const bool uin = vload(&a.state[u]) == MIS_IN;
-            const u32 ru = a.rank[u];
+            const u64 wu = vload64(&a.word[u]);
+            const bool uin = mis_dec(wu) == MIS_IN;
+            const u32 ru = mis_rank(wu);
             const u32 p = V2L(u), np = a.c.ot_size[p], nn = a.c.ot_size[p + 1];
             const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
             for (u32 t = lane; t < np + nn; t += 32)
-                mis_push_one(a, u, ru, uin, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)]), app);
+                mis_push_clause(a, u, ru, uin, hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])]), app);
             __syncwarp();
         }
         const u32* in_s = w.small[wave & 1];
@@ -357,13 +389,15 @@ __global__ void __launch_bounds__(256) mis_waves_k(LcveArgs a, MisWaves w) {
 // B = min(B0, first member whose lists reach the temperatures).
 HD void k_mis_bound(const LcveArgs& a, u32 v) {
     if (v == 0) return;
-    if (a.state[v] == MIS_IN && lcve_big(a, v)) atom_min(&a.bound[1], a.rank[v]);
+    const u64 w = a.word[v];
+    if (mis_rank(w) != NONE && mis_dec(w) == MIS_IN && lcve_big(a, v)) atom_min(&a.bound[1], a.rank[v]);
 }
 
 // Election flags over rank positions below B (compacted by the caller in rank order).
 HD void k_elect_flag(const LcveArgs& a, u32* flags, u32 p) {
     const u32 v = a.order[p];
-    flags[p] = (p < a.bound[1] && a.state[v] == MIS_IN) ? 1u : 0u;
+    const u64 w = a.word[v];
+    flags[p] = (p < a.bound[1] && mis_rank(w) != NONE && mis_dec(w) == MIS_IN) ? 1u : 0u;
 }
 
 HD void k_elect_write(const LcveArgs& a, const u32* flags, const u32* scan, u32 p) {

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 namespace sigma {
 
@@ -220,6 +221,68 @@ struct DBuf {
 };
 
 // Device-time stage timer (CUDA events on the context stream; wall clock in emulation).
+// Device time of one kernel over a round: an event pair around each launch, read
+// once after the round has finished (no synchronisation per launch).
+struct KernelClock {
+#if SIGMA_CUDA
+    std::vector<cudaEvent_t> ev;
+#else
+    std::chrono::steady_clock::time_point t0;
+    double acc = 0;
+#endif
+    size_t used = 0;
+    void start(Runtime& rt) {
+#if SIGMA_CUDA
+        while (used + 2 > ev.size()) {
+            cudaEvent_t e;
+            ck(cudaEventCreate(&e), "event");
+            ev.push_back(e);
+        }
+        ck(cudaEventRecord(ev[used], rt.stream), "event");
+#else
+        (void)rt;
+        t0 = std::chrono::steady_clock::now();
+#endif
+    }
+    void stop(Runtime& rt) {
+#if SIGMA_CUDA
+        ck(cudaEventRecord(ev[used + 1], rt.stream), "event");
+#else
+        (void)rt;
+        acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+#endif
+        used += 2;
+    }
+    u32 launches() const { return (u32)(used / 2); }
+    // Sum over the recorded launches; the stream must have finished them.
+    double total_ms() const {
+#if SIGMA_CUDA
+        double t = 0;
+        for (size_t i = 0; i + 1 < used; i += 2) {
+            float ms = 0;
+            ck(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]), "event time");
+            t += ms;
+        }
+        return t;
+#else
+        return acc;
+#endif
+    }
+    void reset() {
+        used = 0;
+#if !SIGMA_CUDA
+        acc = 0;
+#endif
+    }
+    void destroy() {
+#if SIGMA_CUDA
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+        ev.clear();
+#endif
+        used = 0;
+    }
+};
+
 struct StageTimer {
 #if SIGMA_CUDA
     cudaEvent_t a = nullptr, b = nullptr;

@@ -113,10 +113,11 @@ struct pf_sigma_ctx {
     DBuf<uint8_t> vstate;
     DBuf<u32> trail, resolved;
     DBuf<u32> counters;   // [0] ntrail, [1] err, [2..] scratch counters
-    DBuf<u64> counters64; // [0] nresolved, [1..] scratch
+    DBuf<u64> counters64; // [0] nresolved, [1] elected working set, [2..3] counts, [4] graph working set
     // stage scratch
     DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
-    DBuf<u32> mis_state, mis_big_a, mis_big_b;
+    DBuf<u32> mis_big_a, mis_big_b;
+    DBuf<u64> mis_word;
     DBuf<u32> pv_perm, pv_key;
     DBuf<u32> work, cl_stamp;
     DBuf<u32> radix_hist, radix_hscan, scan_tmp32;
@@ -145,6 +146,11 @@ struct pf_sigma_ctx {
     pf_round_stats st;
     std::vector<uint32_t> dump;
     u64 alg_bytes = 0;
+    // hottest kernels, timed one by one: waves, BVE decision, SUB, BVE write
+    enum { K_MIS, K_BVE, K_SUB, K_BVEW, K_COUNT };
+    KernelClock kclock[K_COUNT];
+    u64 kbytes[K_COUNT] = {};
+    u64 phase_ws = 0;  // elected lists' working set of the current phase
     u32 mis_rounds = 0;
     int bve_mode = 2;  // BVE decision: 0 thread per variable from HBM, 1 thread on a smem copy, 2 warp per variable
 
@@ -372,9 +378,8 @@ struct pf_sigma_ctx {
         a.score = score.p;
         a.order = order.p;
         a.rank = rank.p;
-        a.state = mis_state.p;
-        a.cnt = order_v2.p;    // the radix sort's scratch and sorted keys, free after it
-        a.grank = order_k2.p;
+        a.word = mis_word.p;
+        a.ws_bytes = counters64.p + 4;
         a.bound = bound.p;
         a.pvs = pvs.p;
         rt.zero(score.p, (size_t)(nvars + 1) * 4);
@@ -412,8 +417,11 @@ struct pf_sigma_ctx {
         w.max_waves = nvars + 2;
         rt.zero(ctr + 2, 4 * 4);  // the count-list length in pair 1, and the barrier
         void* args[] = {&a, &w};
+        kclock[K_MIS].start(rt);
         ck(cudaLaunchCooperativeKernel((const void*)mis_waves_k, dim3(mis_waves_grid()), dim3(256), args, 0, rt.stream),
            "cooperative launch");
+        kclock[K_MIS].stop(rt);
+        rt.launches++;
         check();
         rounds = read_u32(ctr + 8);
 #else
@@ -422,6 +430,7 @@ struct pf_sigma_ctx {
         MisFront fout{flags_scan.p, ctr + 2, mis_big_b.p, ctr + 3};
         u32 pend[2];
         rt.d2h(pend, ctr, 8);
+        kclock[K_MIS].start(rt);
         while (pend[0] || pend[1]) {
             if (++rounds > nvars + 2) throw int(PF_ETIMEOUT);
             rt.zero(fout.nsmall, 8);
@@ -430,6 +439,7 @@ struct pf_sigma_ctx {
             std::swap(fin, fout);
             rt.d2h(pend, fin.nsmall, 8);
         }
+        kclock[K_MIS].stop(rt);
 #endif
         mis_rounds += rounds;
         rt.d2d(bound.p + 1, bound.p, 4);
@@ -487,8 +497,11 @@ struct pf_sigma_ctx {
         a.run = nullptr;
         write_u32(counters.p + 5, 0);
         rt.each(FSubPossible{a, counters.p + 5}, npvs);
+        kbytes[K_SUB] += phase_ws;
         if (read_u32(counters.p + 5) == 0) {
+            kclock[K_SUB].start(rt);
             pv_each(FSubPv{a});
+            kclock[K_SUB].stop(rt);
             check();
             return;
         }
@@ -516,7 +529,9 @@ struct pf_sigma_ctx {
         a.units = sub_units.p;
         a.cap_units = (u32)sub_units.n;
         write_u32(counters.p + 4, 0);
+        kclock[K_SUB].start(rt);
         pv_each(FSubPv{a});
+        kclock[K_SUB].stop(rt);
         check();
         u32 nu = read_u32(counters.p + 4);
         if (nu == 0) return;
@@ -662,7 +677,9 @@ struct pf_sigma_ctx {
             }
             ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
             rt.launches++;
+            kclock[K_BVE].start(rt);
             bve_warp_k<<<(u32)rt.sms * 8u, kBveWarpThreads, smem, rt.stream>>>(a, pv_perm.p, counters.p + 11);
+            kclock[K_BVE].stop(rt);
             ck(cudaGetLastError(), "launch");
         } else if (bve_mode == 1) {
             const int smem = kBveThreads * (int)PV_SLOT * 4;
@@ -679,10 +696,13 @@ struct pf_sigma_ctx {
             pv_each(FBveAnalyze{a});
         }
 #else
+        kclock[K_BVE].start(rt);
         if (bve_mode == 2) pv_each(FBveWarp{a});
         else if (bve_mode == 1) pv_each(FBveAnalyzeStaged{a});
         else pv_each(FBveAnalyze{a});
+        kclock[K_BVE].stop(rt);
 #endif
+        kbytes[K_BVE] += phase_ws;
         check();
         const u32 add_cls = scan32(ve_ncls.p, ve_cls_scan.p, npvs);
         const u64 add_lits = scan64(ve_nlits.p, ve_lit_scan.p, npvs);
@@ -697,7 +717,10 @@ struct pf_sigma_ctx {
         a.cls_base = ncls;
         a.lit_base = nlits_used;
         a.wit_base = nresolved;
+        kclock[K_BVEW].start(rt);
         pv_each(FBveWrite{a});
+        kclock[K_BVEW].stop(rt);
+        kbytes[K_BVEW] += phase_ws + 4ull * add_lits + 8ull * add_cls + 4ull * add_wit;
         ncls += add_cls;
         nlits_used += add_lits;
         nresolved += add_wit;
@@ -856,6 +879,7 @@ struct pf_sigma_ctx {
             timed(ST_SORT, &pf_sigma_ctx::sort_ot);
             if (opt.dump_level >= 2) dump_pvlists(phase);
             const u64 W = pv_bytes();
+            phase_ws = W;
             alg_bytes += 2ull * W;  // sort reads and writes the lists (8*occ) ~ bounded by W
             if (stop(diff)) {
                 timed(ST_ERE, &pf_sigma_ctx::ere);
@@ -1009,7 +1033,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         c.pvs.reserve(rt, num_vars + 1);
         c.flags.reserve(rt, num_vars + 1);
         c.flags_scan.reserve(rt, num_vars + 1);
-        c.mis_state.reserve(rt, num_vars + 1);
+        c.mis_word.reserve(rt, num_vars + 1);
         c.radix_hist.reserve(rt, radix_hist_elems(num_vars + 1));
         c.radix_hscan.reserve(rt, radix_hist_elems(num_vars + 1));
         c.scan_tmp32.reserve(rt, scan_tmp_elems(std::max<size_t>(radix_hist_elems(num_vars + 1), cap_cls)) + 4);
@@ -1075,8 +1099,13 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     c.alg_bytes = 0;
     c.mis_rounds = 0;
     c.rt.launches = 0;
+    for (int k = 0; k < pf_sigma_ctx::K_COUNT; k++) {
+        c.kclock[k].reset();
+        c.kbytes[k] = 0;
+    }
     pf_status status = PF_OK;
     try {
+        c.rt.zero(c.counters64.p + 4, 8);
         pf_options& o = c.opt;
         if (c.opt.dump_level > 0) {
             c.dump_cnf(0, 0);
@@ -1112,6 +1141,18 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     c.st.algorithmic_bytes = c.alg_bytes;
     c.st.kernel_launches = c.rt.launches;
     c.st.mis_rounds = c.mis_rounds;
+    if (status == PF_OK || status == PF_UNSAT) {
+        try {
+            c.rt.sync();
+            c.kbytes[pf_sigma_ctx::K_MIS] = c.read_u64(c.counters64.p + 4);
+            for (int k = 0; k < pf_sigma_ctx::K_COUNT; k++) {
+                c.st.ms_kernel[k] = c.kclock[k].total_ms();
+                c.st.bytes_kernel[k] = c.kbytes[k];
+                c.st.launches_kernel[k] = c.kclock[k].launches();
+            }
+        } catch (std::exception&) {
+        }
+    }
     if (stats) *stats = c.st;
     return status;
 }
@@ -1292,7 +1333,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
                         &c.ve_wit_scan, &c.sub_wrd, &c.sub_wrd_off, &c.ere_claim, &c.ere_key};
     for (auto* b : b64) b->free();
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
-    c.mis_state.free();
+    c.mis_word.free();
     c.mis_big_a.free();
     c.mis_big_b.free();
     c.pv_perm.free();
@@ -1301,6 +1342,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     c.sub_units.free();
     c.sub_pairs.free();
     c.tm.destroy();
+    for (auto& k : c.kclock) k.destroy();
     c.rt.destroy();
     delete ctx;
 }

@@ -34,6 +34,10 @@ class SigmaError(RuntimeError):
         self.status = status
 
 
+# The kernels pf_round_stats times one by one (ms_kernel / bytes_kernel order).
+HOT_KERNELS = ("mis_waves", "bve_decide", "sub", "bve_write")
+
+
 class RoundStats(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("phases_run", ctypes.c_int32),
                 ("clauses_before", ctypes.c_uint64), ("literals_before", ctypes.c_uint64),
@@ -42,11 +46,15 @@ class RoundStats(ctypes.Structure):
                 ("resolved_words", ctypes.c_uint64), ("ms_total", ctypes.c_double),
                 ("ms_stage", ctypes.c_double * 12), ("algorithmic_bytes", ctypes.c_uint64),
                 ("kernel_launches", ctypes.c_uint32), ("mis_rounds", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 2)]
+                ("reserved", ctypes.c_uint32 * 2), ("ms_kernel", ctypes.c_double * 4),
+                ("bytes_kernel", ctypes.c_uint64 * 4), ("launches_kernel", ctypes.c_uint32 * 4)]
 
     def as_dict(self) -> dict:
-        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("ms_stage", "reserved")}
+        d = {f: getattr(self, f) for f, _ in self._fields_
+             if f not in ("ms_stage", "reserved", "ms_kernel", "bytes_kernel", "launches_kernel")}
         d["ms_stage"] = {s: self.ms_stage[i] for i, s in enumerate(STAGES)}
+        d["kernels"] = {k: {"ms": self.ms_kernel[i], "bytes": int(self.bytes_kernel[i]),
+                            "launches": int(self.launches_kernel[i])} for i, k in enumerate(HOT_KERNELS)}
         return d
 
 
