@@ -161,6 +161,36 @@ pf_status pf_create_ot_noalloc(uint32_t num_vars, const uint32_t* d_lits, const 
                                uint64_t num_clauses, uint32_t* d_ot_off, uint32_t* d_ot_size, uint32_t* d_ot_refs,
                                void* stream);
 
+/* ---- Formula batches (no counterpart in the reference: ParaFROST simplifies one
+ * formula per solver object; many small formulas are simplified here by one context).
+ * Formula f has num_vars[f] variables and the clauses [clause_begin[f], clause_begin[f+1])
+ * of lits/offsets (clause_begin[0] = 0), its literals in its own numbering
+ * (2v + sign, 1 <= v <= num_vars[f]); num_vars and clause_begin are host arrays of
+ * num_formulas and num_formulas + 1 entries. pf_sigma_round then runs every formula's
+ * own round (its own phases, stop rule and bounds, as pf_sigma_round on that formula
+ * alone would) on the one resident store; a formula that derives the empty clause
+ * ends with status PF_UNSAT while the others go on. No learnt clauses, no dumps. */
+pf_status pf_sigma_upload_batch(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
+                                const uint64_t* clause_begin, const uint32_t* lits, const uint64_t* offsets);
+
+/* Same as pf_sigma_upload_batch with lits/offsets in device memory. */
+pf_status pf_sigma_upload_batch_device(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
+                                       const uint64_t* clause_begin, const uint32_t* d_lits,
+                                       const uint64_t* d_offsets);
+
+/* Per formula of the last batched round (arrays of num_formulas; any may be NULL):
+ * status (PF_OK or PF_UNSAT), phases run, and the sizes pf_sigma_batch_download
+ * writes for that formula. */
+pf_status pf_sigma_batch_result_sizes(pf_sigma_ctx* ctx, int32_t* status, uint32_t* phases, uint64_t* num_clauses,
+                                      uint64_t* num_literals, uint64_t* num_units, uint64_t* num_resolved);
+
+/* Every formula's result, formula after formula, in its own numbering (any pointer
+ * may be NULL): clauses (lits, offsets with sum(num_clauses) + 1 entries into lits,
+ * learnt), trail units, witness stack, and num_vars[f] + 1 eliminated flags per
+ * formula (the first of each unused), with the layouts of pf_sigma_download. */
+pf_status pf_sigma_batch_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets, uint8_t* learnt,
+                                  uint32_t* units, uint32_t* resolved, uint8_t* eliminated);
+
 /* Device bytes held by the context. */
 pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes);
 

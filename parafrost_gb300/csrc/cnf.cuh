@@ -72,6 +72,10 @@ struct Ctx {
     u64 cap_resolved;
     // error word
     u32* err;
+    // formula batches (null for a single formula): formula of each variable, and
+    // one error word per formula (an empty clause ends that formula only)
+    const u32* var_fid;
+    u32* f_err;
 };
 
 constexpr u32 NONE = 0xFFFFFFFFu;
@@ -83,6 +87,13 @@ HD int lit_value(const Ctx& c, u32 lit) {
 }
 
 HD void set_err(const Ctx& c, u32 bits) { atom_or(c.err, bits); }
+
+// The formula holding variable v derived the empty clause.
+HD void set_unsat(const Ctx& c, u32 v) {
+    if (c.var_fid) atom_or(&c.f_err[c.var_fid[v]], ERR_UNSAT);
+    else set_err(c, ERR_UNSAT);
+}
+HD u32 fid_of(const Ctx& c, u32 v) { return c.var_fid ? c.var_fid[v] : 0u; }
 
 // Header load through the read-only path (for launches that write no header).
 HD Hdr hdr_ro(const Hdr* p) {

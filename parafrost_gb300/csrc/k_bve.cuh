@@ -211,7 +211,7 @@ HD void enqueue_unit(const Ctx& c, u32 u) {
         const u32 pos = atom_add(c.ntrail, 1u);
         c.trail[pos] = u;
     } else if (old != u) {
-        set_err(c, ERR_UNSAT);
+        set_unsat(c, ABS(u));
     }
 }
 

@@ -38,7 +38,9 @@ struct LcveArgs {
     u32* rank;            // nvars+1
     u64* word;            // nvars+1: independent-set words
     u64* ws_bytes;        // accumulates the graph's working set (4*occ + sum(8 + 4*len))
-    u32* bound;           // [0] = B0 (first valid non-F rank), [1] = B
+    u32* bound;           // per formula f: [2f] = B0 (first valid non-F rank), [2f+1] = B
+    const u32* f_active;  // batches: formulas taking part in this election (null: all)
+    u32* f_npvs;          // batches: elected variables per formula
     u32* pvs;             // elected variables in rank order
 };
 
@@ -62,7 +64,7 @@ HD bool lcve_big(const LcveArgs& a, u32 v) {
 HD void k_rank(const LcveArgs& a, u32 p) {
     const u32 v = a.order[p];
     a.rank[v] = p;
-    if (lcve_valid(a.c, v) && !lcve_freezable(a, v)) atom_min(&a.bound[0], p);
+    if (lcve_valid(a.c, v) && !lcve_freezable(a, v)) atom_min(&a.bound[2 * fid_of(a.c, v)], p);
 }
 
 // The independent set is decided by pushing decisions along edges to higher ranks:
@@ -94,7 +96,9 @@ HD void mis_append(const MisFront& f, const Ctx& c, u32 v, bool pred) {
 
 // Graph membership, and the list of large graph vertices for the warp count.
 HD void k_mis_init(const LcveArgs& a, const MisFront& bigs, u32 v) {
-    const bool in_graph = v && lcve_valid(a.c, v) && lcve_freezable(a, v) && a.rank[v] < a.bound[0];
+    const u32 f = v ? fid_of(a.c, v) : 0u;
+    const bool in_graph = v && (!a.f_active || a.f_active[f]) && lcve_valid(a.c, v) && lcve_freezable(a, v) &&
+                          a.rank[v] < a.bound[2 * f];
     a.word[v] = in_graph ? a.rank[v] : NONE;
     const bool big = in_graph && mis_is_big(a.c, v);
     const u32 pb = warp_append(bigs.nbig, big);
@@ -386,18 +390,21 @@ __global__ void __launch_bounds__(256) mis_waves_k(LcveArgs a, MisWaves w) {
 }
 #endif
 
+// B starts at B0, per formula.
+HD void k_bound_init(const LcveArgs& a, u32 f) { a.bound[2 * f + 1] = a.bound[2 * f]; }
+
 // B = min(B0, first member whose lists reach the temperatures).
 HD void k_mis_bound(const LcveArgs& a, u32 v) {
     if (v == 0) return;
     const u64 w = a.word[v];
-    if (mis_rank(w) != NONE && mis_dec(w) == MIS_IN && lcve_big(a, v)) atom_min(&a.bound[1], a.rank[v]);
+    if (mis_rank(w) != NONE && mis_dec(w) == MIS_IN && lcve_big(a, v)) atom_min(&a.bound[2 * fid_of(a.c, v) + 1], a.rank[v]);
 }
 
 // Election flags over rank positions below B (compacted by the caller in rank order).
 HD void k_elect_flag(const LcveArgs& a, u32* flags, u32 p) {
     const u32 v = a.order[p];
     const u64 w = a.word[v];
-    flags[p] = (p < a.bound[1] && mis_rank(w) != NONE && mis_dec(w) == MIS_IN) ? 1u : 0u;
+    flags[p] = (p < a.bound[2 * fid_of(a.c, v) + 1] && mis_rank(w) != NONE && mis_dec(w) == MIS_IN) ? 1u : 0u;
 }
 
 HD void k_elect_write(const LcveArgs& a, const u32* flags, const u32* scan, u32 p) {
@@ -405,6 +412,7 @@ HD void k_elect_write(const LcveArgs& a, const u32* flags, const u32* scan, u32 
     const u32 v = a.order[p];
     a.pvs[scan[p]] = v;
     a.c.pvrank[v] = scan[p];
+    if (a.f_npvs) atom_add(&a.f_npvs[fid_of(a.c, v)], 1u);
 }
 
 }  // namespace sigma

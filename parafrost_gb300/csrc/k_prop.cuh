@@ -62,6 +62,7 @@ HD void k_prop_clause(const PropArgs& a, u32 k) {
     Hdr h = c.hdr[r];
     if (h_deleted(h.flags)) return;
     u32* l = c.lits + h.start;
+    const u32 v0 = ABS(l[0]);  // names the formula if the clause empties
     // satisfied?
     for (u32 i = 0; i < h.size; i++) {
         if (lit_value(c, l[i]) == 1) {
@@ -79,7 +80,12 @@ HD void k_prop_clause(const PropArgs& a, u32 k) {
     h.size = n;
     h.sig = sig;
     c.hdr[r] = h;
-    if (n == 0) { set_err(c, ERR_UNSAT); return; }
+    if (n == 0) {
+        set_unsat(c, v0);
+        // in a batch the other formulas go on: keep no empty live clause around
+        if (c.var_fid) c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+        return;
+    }
     if (n == 1) {
         const u32 u = l[0];
         const u32 old = atom_cas(&c.asg[ABS(u)], 0u, u);
@@ -87,7 +93,7 @@ HD void k_prop_clause(const PropArgs& a, u32 k) {
             const u32 pos = atom_add(c.ntrail, 1u);
             c.trail[pos] = u;
         } else if (old != u) {
-            set_err(c, ERR_UNSAT);
+            set_unsat(c, ABS(u));
         }
     }
 }

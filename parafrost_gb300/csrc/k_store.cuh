@@ -17,13 +17,40 @@ struct UploadArgs {
     const u64* off;      // num_clauses + 1
     const uint8_t* learnt;  // may be null
     u64 base;            // literal offset of off[0]
+    // formula batches: nf formulas, formula f holds clauses [f_cls[f], f_cls[f+1])
+    // and f_nv[f] variables from f_var[f]+1 on; its literals arrive in its own
+    // numbering and are moved to the batch's (nf = 0: a single formula)
+    u32 nf;
+    const u64* f_cls;
+    const u32* f_var;
+    const u32* f_nv;
 };
+
+// Largest f < n with start[f] <= key (start ascending, start[0] <= key).
+template <class T>
+HD u32 upper_segment(const T* start, u32 n, T key) {
+    u32 lo = 0, hi = n;  // answer in [lo, hi)
+    while (hi - lo > 1) {
+        const u32 mid = (lo + hi) >> 1;
+        if (start[mid] <= key) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
 
 HD void k_upload_clause(const UploadArgs& a, u32 i) {
     const u64 s = a.off[i] - a.base, e = a.off[i + 1] - a.base;
     u32* l = a.c.lits + s;
     const u32 n = (u32)(e - s);
     if (n == 0) { set_err(a.c, ERR_INPUT); return; }
+    if (a.nf) {
+        const u32 f = upper_segment(a.f_cls, a.nf, (u64)i);
+        const u32 shift = 2u * a.f_var[f], lim = 2u * a.f_nv[f] + 2u;
+        for (u32 k = 0; k < n; k++) {
+            if (l[k] < 2 || l[k] >= lim) { set_err(a.c, ERR_INPUT); return; }
+            l[k] += shift;
+        }
+    }
     if (n <= 32) ref_insertion_sort(l, (int)n, LitLess());
     else std_sort_replica(l, l + n, LitLess());
     u32 sig = 0;
@@ -125,7 +152,52 @@ HD void k_count_clause(const CountArgs& a, u32 i) {
     atom_add64(&a.out[1], (u64)h.size);
 }
 
+// Formula of every variable of a batch (variable 0 belongs to none).
+HD void k_var_fid(u32* var_fid, const u32* f_var, u32 nf, u32 v) {
+    var_fid[v] = v ? upper_segment(f_var, nf, v - 1) : NONE;
+}
+
+// Live clauses and literals per formula of a batch (countAll per formula); a
+// clause's formula is that of its first literal's variable.
+struct FormulaCountArgs {
+    Ctx c;
+    u64* f_cls;   // nf
+    u64* f_lits;  // nf
+};
+HD void k_count_formula(const FormulaCountArgs& a, u32 i) {
+    const Hdr h = a.c.hdr[i];
+    if (h_deleted(h.flags)) return;
+    const u32 f = a.c.var_fid[ABS(a.c.lits[h.start])];
+    atom_add64(&a.f_cls[f], 1ull);
+    atom_add64(&a.f_lits[f], (u64)h.size);
+}
+
 #if SIGMA_CUDA
+// Same count; lanes of a warp that share a formula (a formula's clauses are
+// mostly adjacent) add once.
+__global__ void count_formula_k(FormulaCountArgs a, u32 n) {
+    const u32 lane = threadIdx.x & 31u;
+    for (u32 base = blockIdx.x * blockDim.x; base < n; base += blockDim.x * gridDim.x) {
+        const u32 i = base + threadIdx.x;
+        u32 f = NONE, cls = 0, lits = 0;
+        if (i < n) {
+            const Hdr h = a.c.hdr[i];
+            if (!h_deleted(h.flags)) {
+                f = a.c.var_fid[ABS(a.c.lits[h.start])];
+                cls = 1;
+                lits = h.size;
+            }
+        }
+        const u32 peers = __match_any_sync(0xffffffffu, f);
+        cls = __reduce_add_sync(peers, cls);
+        lits = __reduce_add_sync(peers, lits);
+        if (f != NONE && lane == (u32)(__ffs(peers) - 1)) {
+            atomicAdd((unsigned long long*)&a.f_cls[f], (unsigned long long)cls);
+            atomicAdd((unsigned long long*)&a.f_lits[f], (unsigned long long)lits);
+        }
+    }
+}
+
 // Same counts with a warp/block reduction and one pair of atomics per block.
 __global__ void count_live_k(const Hdr* __restrict__ hdr, u32 n, u64* out) {
     u64 cls = 0, lits = 0;

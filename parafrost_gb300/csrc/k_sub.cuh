@@ -137,7 +137,7 @@ HD void sub_strengthen(const SubArgs& a, u32 k, u32 p, u32 r, u32 me, SubLocal& 
             else set_err(c, ERR_CAP_SCRATCH);
             sub_local_oblivion(c, p, unit);
         } else if (val == 0) {
-            set_err(c, ERR_UNSAT);
+            set_unsat(c, ABS(unit));
         }
     }
 }

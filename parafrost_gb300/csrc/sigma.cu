@@ -16,6 +16,7 @@
 #include "runtime.h"
 
 #include <algorithm>
+#include <array>
 #include <climits>
 #include <map>
 #include <mutex>
@@ -79,12 +80,40 @@ struct Perm {
     HD void operator()(u32 i) const { f(perm[i]); }
 };
 // Work-order key of elected variable k: descending clause count.
+// Elected variables from n_first on (a batch's stopping formulas) come after the
+// others.
 struct FPvKey {
-    Ctx c; const u32* pvs; u32* key; u32* val;
+    Ctx c; const u32* pvs; u32* key; u32* val; u32 n_first;
     HD void operator()(u32 k) const {
         const u32 p = V2L(pvs[k]);
-        key[k] = 0xFFFFFFFFu - (c.ot_size[p] + c.ot_size[p + 1]);
+        const u32 occ = c.ot_size[p] + c.ot_size[p + 1];
+        key[k] = (k >= n_first ? 0x80000000u : 0u) | (0x7FFFFFFFu - (occ < 0x7FFFFFFFu ? occ : 0x7FFFFFFFu));
         val[k] = k;
+    }
+};
+struct FBoundInit { LcveArgs a; HD void operator()(u32 f) const { k_bound_init(a, f); } };
+struct FVarFid { u32* var_fid; const u32* f_var; u32 nf; HD void operator()(u32 v) const { k_var_fid(var_fid, f_var, nf, v); } };
+struct FCountFormula { FormulaCountArgs a; HD void operator()(u32 i) const { k_count_formula(a, i); } };
+// Batch partition of the elected list: group of each elected variable's formula
+// (0 dropped, 1 goes on, 2 stops this phase).
+struct FPvGroup {
+    Ctx c; const u32* pvs; const u32* f_group; u32* go; u32* stop;
+    HD void operator()(u32 k) const {
+        const u32 g = f_group[fid_of(c, pvs[k])];
+        go[k] = g == 1u;
+        stop[k] = g == 2u;
+    }
+};
+struct FPvPartition {
+    Ctx c; const u32* pvs; const u32* go; const u32* go_scan; const u32* stop; const u32* stop_scan; u32 n_go;
+    u32* out;
+    HD void operator()(u32 k) const {
+        const u32 v = pvs[k];
+        u32 pos = NONE;
+        if (go[k]) pos = go_scan[k];
+        else if (stop[k]) pos = n_go + stop_scan[k];
+        if (pos != NONE) out[pos] = v;
+        c.pvrank[v] = pos;
     }
 };
 
@@ -137,8 +166,18 @@ struct pf_sigma_ctx {
     // ERE
     DBuf<u64> ere_claim, ere_key;
     DBuf<u32> ere_target, ere_losers;
+    // formula batch (nf = 0: one formula). Formula f owns variables
+    // h_f_var[f]+1 .. h_f_var[f+1] of the store's numbering.
+    u32 nf = 0;
+    std::vector<u32> h_f_var, h_f_nv;
+    DBuf<u32> f_var, var_fid, f_err, f_active, f_npvs, f_group;
+    DBuf<u64> f_count;  // [f] live clauses, [nf + f] live literals
+    std::vector<int> f_status;
+    std::vector<u32> f_phases;
     // host state
     u32 npvs = 0;
+    u32 n_go = 0;                  // elected variables of the formulas that go on (front of pvs)
+    u32 perm_off = 0, perm_n = 0;  // range of pv_perm the per-variable stages run over
     bool ot_dirty = false;  // clauses changed since the OT build
     int phase = 0;
     u32 mu_inc = 0;
@@ -180,6 +219,8 @@ struct pf_sigma_ctx {
         c.nresolved = counters64.p + 0;
         c.cap_resolved = resolved.n;
         c.err = counters.p + 1;
+        c.var_fid = nf ? var_fid.p : nullptr;
+        c.f_err = nf ? f_err.p : nullptr;
         return c;
     }
 
@@ -382,6 +423,9 @@ struct pf_sigma_ctx {
         a.ws_bytes = counters64.p + 4;
         a.bound = bound.p;
         a.pvs = pvs.p;
+        a.f_active = nf ? f_active.p : nullptr;
+        a.f_npvs = nf ? f_npvs.p : nullptr;
+        const u32 nform = nf ? nf : 1u;
         rt.zero(score.p, (size_t)(nvars + 1) * 4);
         rt.each(FScores{a}, nvars + 1);
         // LCV order: stable by score over ascending variables (rSort, sort.h:123-133)
@@ -389,8 +433,7 @@ struct pf_sigma_ctx {
         radix_sort_pairs(order_k2.p, order.p, order_v2.p, rank.p, nvars, 32, radix_hist.p, radix_hscan.p,
                          scan_tmp32.p, rt.stream);
         rt.launches += 20;
-        u32 init_b[2] = {NONE, NONE};
-        rt.h2d(bound.p, init_b, 8);
+        rt.zero(bound.p, (size_t)nform * 8, 0xFF);
         rt.each(FRank{a}, nvars);
         // Independent set by frontier waves. The frontier lists (small / large
         // adjacency) alternate between flags|mis_big_a and flags_scan|mis_big_b.
@@ -442,12 +485,16 @@ struct pf_sigma_ctx {
         kclock[K_MIS].stop(rt);
 #endif
         mis_rounds += rounds;
-        rt.d2d(bound.p + 1, bound.p, 4);
+        rt.each(FBoundInit{a}, nform);
         rt.each(FMisBound{a}, nvars + 1);
         rt.each(FFill32{pvrank.p, NONE}, nvars + 1);
         rt.each(FElectFlag{a, flags.p}, nvars);
+        if (nf) rt.zero(f_npvs.p, (size_t)nf * 4);
         npvs = scan32(flags.p, flags_scan.p, nvars);
         rt.each(FElectWrite{a, flags.p, flags_scan.p}, nvars);
+        n_go = npvs;
+        perm_off = 0;
+        perm_n = npvs;
         alg_bytes += 4ull * D + 24ull * nvars;
         if (opt.dump_level >= 2) {
             rec(3, phase, 2, fetch(score.p, nvars + 1));
@@ -466,7 +513,7 @@ struct pf_sigma_ctx {
         // ones do not start last. Results still go to each variable's elected rank.
         pv_perm.reserve(rt, nvars + 1);
         pv_key.reserve(rt, nvars + 1);
-        rt.each(FPvKey{view(), pvs.p, pv_key.p, pv_perm.p}, npvs);
+        rt.each(FPvKey{view(), pvs.p, pv_key.p, pv_perm.p, n_go}, npvs);
         radix_sort_pairs(pv_key.p, pv_perm.p, order_k2.p, order_v2.p, npvs, 32, radix_hist.p, radix_hscan.p,
                          scan_tmp32.p, rt.stream);
         rt.launches += 20;
@@ -475,7 +522,7 @@ struct pf_sigma_ctx {
     // f(k) for every elected variable, in work order, dynamically scheduled.
     template <class F>
     void pv_each(const F& f) {
-        rt.each_dyn(Perm<F>{f, pv_perm.p}, npvs, counters.p + 11);
+        rt.each_dyn(Perm<F>{f, pv_perm.p + perm_off}, perm_n, counters.p + 11);
     }
 
     // working set of the elected lists, accumulated by the sort kernel
@@ -619,7 +666,12 @@ struct pf_sigma_ctx {
         for (const U2& u : units) {
             const u32 lit = u.y, v = ABS(lit);
             if (A[v] == 0) { A[v] = lit; tr.push_back(lit); ul.push_back(lit); }
-            else if (A[v] != lit) throw int(PF_UNSAT);
+            else if (A[v] != lit) {
+                if (!nf) throw int(PF_UNSAT);
+                const u32 f = read_u32(var_fid.p + v);  // that formula alone is unsatisfiable
+                const u32 bit = ERR_UNSAT;
+                rt.h2d(f_err.p + f, &bit, 4);
+            }
         }
         for (u32 lit : tr) write_u32(asg.p + ABS(lit), lit);
         if (!tr.empty()) {
@@ -910,6 +962,160 @@ struct pf_sigma_ctx {
         timed(ST_GC, &pf_sigma_ctx::gc);
         st.phases_run = phase;
     }
+
+    // ------------------------------------------------------------ formula batches
+    // Each formula of a batch runs its own sigmifying loop; the formulas share the
+    // store, so one phase does the stage kernels once for all formulas still in their
+    // loop. Formulas never share variables or clauses, so every stage's result for a
+    // formula is the one it would have alone: the election's order restricted to a
+    // formula is that formula's own (score, variable) order, its bounds are kept per
+    // formula, and new clauses and witness words keep each formula's relative order.
+    // A formula leaves the loop exactly where its own would end; its final
+    // propagation then happens in the next phase's (or the closing) propagation.
+    std::vector<u64> fc_cls, fc_lits;
+
+    void count_formulas() {
+        rt.zero(f_count.p, (size_t)nf * 16);
+        FormulaCountArgs a{view(), f_count.p, f_count.p + nf};
+#if SIGMA_CUDA
+        if (ncls) {
+            rt.launches++;
+            count_formula_k<<<rt.grid(ncls, 4), 256, 0, rt.stream>>>(a, ncls);
+            ck(cudaGetLastError(), "launch");
+        }
+#else
+        rt.each(FCountFormula{a}, ncls);
+#endif
+        std::vector<u64> h = fetch(f_count.p, 2 * (size_t)nf);
+        fc_cls.assign(h.begin(), h.begin() + nf);
+        fc_lits.assign(h.begin() + nf, h.end());
+        n_cls_after = n_lits_after = 0;
+        for (u32 f = 0; f < nf; f++) {
+            n_cls_after += (i64)fc_cls[f];
+            n_lits_after += (i64)fc_lits[f];
+        }
+    }
+
+    // Formulas that derived the empty clause leave the loop with status UNSAT.
+    void mark_unsat(std::vector<uint8_t>& done) {
+        const std::vector<u32> e = fetch(f_err.p, nf);
+        for (u32 f = 0; f < nf; f++) {
+            if ((e[f] & ERR_UNSAT) && f_status[f] != PF_UNSAT) {
+                f_status[f] = PF_UNSAT;
+                f_phases[f] = 0;  // as a single round stopped by the empty clause reports
+                done[f] = 1;
+            }
+        }
+    }
+
+    // Orders the elected list as [formulas that go on | formulas that stop this
+    // phase]; elected variables of dropped formulas leave it. group: per formula.
+    void partition_pvs(const std::vector<u32>& group) {
+        rt.h2d(f_group.p, group.data(), (size_t)nf * 4);
+        big32a.reserve(rt, (size_t)npvs + 1);
+        big32b.reserve(rt, (size_t)npvs + 1);
+        const Ctx c = view();
+        rt.each(FPvGroup{c, pvs.p, f_group.p, flags.p, big32a.p}, npvs);
+        const u32 ngo = scan32(flags.p, flags_scan.p, npvs);
+        const u32 nstop = scan32(big32a.p, big32b.p, npvs);
+        pv_key.reserve(rt, nvars + 1);
+        rt.each(FPvPartition{c, pvs.p, flags.p, flags_scan.p, big32a.p, big32b.p, ngo, pv_key.p}, npvs);
+        rt.d2d(pvs.p, pv_key.p, (size_t)(ngo + nstop) * 4);
+        npvs = ngo + nstop;
+        n_go = ngo;
+    }
+
+    void round_batch() {
+        phase = 0;
+        mu_inc = 0;
+        std::fill(f_status.begin(), f_status.end(), (int)PF_OK);
+        std::fill(f_phases.begin(), f_phases.end(), 0u);
+        std::vector<uint8_t> done(nf, 0);
+        count_formulas();
+        st.clauses_before = (u64)n_cls_after;
+        st.literals_before = (u64)n_lits_after;
+        const pf_options& o = opt;
+        if (!o.phases && !(o.all || o.ere)) return;
+        std::vector<i64> litsbefore(nf), diff(nf, INT64_MAX);
+        for (u32 f = 0; f < nf; f++) {
+            litsbefore[f] = (i64)fc_lits[f];
+            if (!litsbefore[f]) done[f] = 1;
+        }
+        std::vector<u32> active(nf), group(nf);
+        for (;;) {
+            bool any = false;
+            for (u32 f = 0; f < nf; f++) any |= !done[f];
+            if (!any) break;
+            timed(ST_GC, &pf_sigma_ctx::resize_cnf);
+            timed(ST_OT, &pf_sigma_ctx::create_ot);
+            timed(ST_PROP, &pf_sigma_ctx::prop);
+            mark_unsat(done);
+            for (u32 f = 0; f < nf; f++) active[f] = !done[f];
+            rt.h2d(f_active.p, active.data(), (size_t)nf * 4);
+            tm.start(rt);
+            lcve();
+            const std::vector<u32> fn = fetch(f_npvs.p, nf);
+            u32 going = 0;
+            for (u32 f = 0; f < nf; f++) {
+                group[f] = 0;
+                if (done[f]) continue;
+                if (fn[f] < (u32)o.lcve_min) {  // LCVE() false: leave the loop
+                    done[f] = 1;
+                    f_phases[f] = (u32)phase;
+                } else {
+                    group[f] = stop(diff[f]) ? 2u : 1u;
+                    going++;
+                }
+            }
+            partition_pvs(group);
+            st.ms_stage[ST_LCVE] += tm.stop(rt);
+            if (!going) continue;
+            timed(ST_SORT, &pf_sigma_ctx::sort_ot);
+            const u64 W = pv_bytes();
+            phase_ws = W;
+            alg_bytes += 2ull * W;
+            const u32 all = npvs;
+            if (n_go < all) {  // stop(diff): ERE, then leave the loop
+                perm_off = n_go;
+                perm_n = all - n_go;
+                timed(ST_ERE, &pf_sigma_ctx::ere);
+            }
+            if (n_go) {
+                npvs = n_go;
+                perm_off = 0;
+                perm_n = n_go;
+                timed(ST_SUB, &pf_sigma_ctx::sub);
+                timed(ST_VE, &pf_sigma_ctx::ve);
+                timed(ST_BCE, &pf_sigma_ctx::bce);
+                npvs = all;
+            }
+            alg_bytes += 4ull * W;
+            timed(ST_COUNT, &pf_sigma_ctx::count_formulas);
+            mark_unsat(done);
+            for (u32 f = 0; f < nf; f++) {
+                if (done[f]) continue;
+                if (group[f] == 2) {
+                    done[f] = 1;
+                    f_phases[f] = (u32)phase;
+                } else if (group[f] == 1) {
+                    diff[f] = litsbefore[f] - (i64)fc_lits[f];
+                    litsbefore[f] = (i64)fc_lits[f];
+                    if (!litsbefore[f]) {
+                        done[f] = 1;
+                        f_phases[f] = (u32)phase + 1;
+                    }
+                }
+            }
+            phase++;
+            mu_inc++;
+            mu_inc += (phase == o.phases);
+        }
+        timed(ST_PROP, &pf_sigma_ctx::prop);
+        timed(ST_COUNT, &pf_sigma_ctx::count_formulas);
+        mark_unsat(done);
+        timed(ST_GC, &pf_sigma_ctx::gc);
+        st.phases_run = phase;
+    }
 };
 
 // ---------------------------------------------------------------- C ABI
@@ -979,8 +1185,27 @@ pf_status pf_sigma_create(const pf_options* opts, pf_sigma_ctx** out) {
     return PF_OK;
 }
 
+// Variable offsets of a batch's formulas in the store's numbering. Each formula's
+// range starts at a multiple of 16 variables, so its literals move by a multiple of
+// 32 and keep their signature bits (1 << (lit & 31)): clause signatures, and the
+// occurrence-list order they take part in, are the formula's own.
+static std::vector<u32> batch_var_offsets(u32 nf, const uint32_t* num_vars) {
+    std::vector<u32> off(nf + 1, 0);
+    for (u32 f = 0; f < nf; f++) off[f + 1] = off[f] + ((num_vars[f] + 15u) & ~15u);
+    return off;
+}
+
+// Formula batch of an upload: nf formulas with their variable counts and clause
+// ranges (host arrays).
+struct BatchSpec {
+    u32 nf;
+    const uint32_t* num_vars;
+    const uint64_t* clause_begin;
+};
+
 static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint32_t* lits, const uint64_t* offsets,
-                               uint64_t num_clauses, const uint8_t* learnt, bool device) {
+                               uint64_t num_clauses, const uint8_t* learnt, bool device,
+                               const BatchSpec* batch = nullptr) {
     if (!ctx) return fail("null context", PF_EINVAL);
     if (!lits || !offsets || num_vars == 0) return fail("null formula", PF_EINVAL);
     if (num_vars >= (1u << 30)) return fail("too many variables", PF_EINVAL);
@@ -1001,6 +1226,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         if (L >= 0xF0000000ull) return fail("too many literals", PF_EINVAL);
         c.nvars = num_vars;
         c.D = 2 * (num_vars + 1);
+        c.nf = batch ? batch->nf : 0u;
         c.ncls = (u32)num_clauses;
         c.nlits_used = L;
         c.ntrail = c.prop_head = 0;
@@ -1029,7 +1255,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         c.order_k2.reserve(rt, num_vars + 1);
         c.order_v2.reserve(rt, num_vars + 1);
         c.rank.reserve(rt, num_vars + 1);
-        c.bound.reserve(rt, 4);
+        c.bound.reserve(rt, 4);  // a batch upload widens it to two words per formula
         c.pvs.reserve(rt, num_vars + 1);
         c.flags.reserve(rt, num_vars + 1);
         c.flags_scan.reserve(rt, num_vars + 1);
@@ -1065,11 +1291,38 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
             else std::memcpy(h.data(), learnt, num_clauses);
             for (u64 i = 0; i < num_clauses; i++) if (h[i]) { c.has_learnt = true; break; }
         }
-        UploadArgs a{c.view(), off_ptr, learnt_ptr, off0};
+        DBuf<u64> dcls;
+        DBuf<u32> dnv;
+        UploadArgs a{c.view(), off_ptr, learnt_ptr, off0, 0u, nullptr, nullptr, nullptr};
+        if (batch) {
+            const u32 nf = batch->nf;
+            c.h_f_var = batch_var_offsets(nf, batch->num_vars);
+            c.h_f_nv.assign(batch->num_vars, batch->num_vars + nf);
+            c.f_var.reserve(rt, nf + 1);
+            rt.h2d(c.f_var.p, c.h_f_var.data(), (size_t)(nf + 1) * 4);
+            dnv.reserve(rt, nf);
+            rt.h2d(dnv.p, batch->num_vars, (size_t)nf * 4);
+            dcls.reserve(rt, nf + 1);
+            rt.h2d(dcls.p, batch->clause_begin, (size_t)(nf + 1) * 8);
+            c.var_fid.reserve(rt, num_vars + 1);
+            rt.each(FVarFid{c.var_fid.p, c.f_var.p, nf}, num_vars + 1);
+            c.f_err.reserve(rt, nf);
+            rt.zero(c.f_err.p, (size_t)nf * 4);
+            c.f_active.reserve(rt, nf);
+            c.f_npvs.reserve(rt, nf);
+            c.f_group.reserve(rt, nf);
+            c.f_count.reserve(rt, 2 * (size_t)nf);
+            c.bound.reserve(rt, 2 * (size_t)nf + 2);
+            c.f_status.assign(nf, PF_OK);
+            c.f_phases.assign(nf, 0);
+            a = UploadArgs{c.view(), off_ptr, learnt_ptr, off0, nf, dcls.p, c.f_var.p, dnv.p};
+        }
         rt.each(FUpload{a}, (u32)num_clauses);
         rt.sync();
         doff.free();
         dlearnt.free();
+        dcls.free();
+        dnv.free();
         const u32 e = c.read_err();
         if (e & ERR_INPUT) {
             c.uploaded = false;
@@ -1088,6 +1341,34 @@ pf_status pf_sigma_upload(pf_sigma_ctx* ctx, uint32_t num_vars, const uint32_t* 
 pf_status pf_sigma_upload_device(pf_sigma_ctx* ctx, uint32_t num_vars, const uint32_t* d_lits,
                                  const uint64_t* d_offsets, uint64_t num_clauses, const uint8_t* d_learnt) {
     return upload_common(ctx, num_vars, d_lits, d_offsets, num_clauses, d_learnt, true);
+}
+
+static pf_status upload_batch(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
+                              const uint64_t* clause_begin, const uint32_t* lits, const uint64_t* offsets, bool device) {
+    if (!ctx) return fail("null context", PF_EINVAL);
+    if (!num_formulas || !num_vars || !clause_begin) return fail("empty batch", PF_EINVAL);
+    if (clause_begin[0] != 0) return fail("clause_begin[0] must be 0", PF_EINVAL);
+    u64 total_vars = 0;
+    for (u32 f = 0; f < num_formulas; f++) {
+        if (clause_begin[f + 1] < clause_begin[f]) return fail("clause ranges not ascending", PF_EINVAL);
+        if (num_vars[f] >= (1u << 30)) return fail("too many variables", PF_EINVAL);
+        total_vars += (num_vars[f] + 15u) & ~15u;
+    }
+    if (total_vars == 0) return fail("batch without variables", PF_EINVAL);
+    if (total_vars >= (1u << 30)) return fail("too many variables", PF_EINVAL);
+    BatchSpec b{num_formulas, num_vars, clause_begin};
+    return upload_common(ctx, (u32)total_vars, lits, offsets, clause_begin[num_formulas], nullptr, device, &b);
+}
+
+pf_status pf_sigma_upload_batch(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
+                                const uint64_t* clause_begin, const uint32_t* lits, const uint64_t* offsets) {
+    return upload_batch(ctx, num_formulas, num_vars, clause_begin, lits, offsets, false);
+}
+
+pf_status pf_sigma_upload_batch_device(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
+                                       const uint64_t* clause_begin, const uint32_t* d_lits,
+                                       const uint64_t* d_offsets) {
+    return upload_batch(ctx, num_formulas, num_vars, clause_begin, d_lits, d_offsets, true);
 }
 
 pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
@@ -1114,7 +1395,12 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
         StageTimer whole;
         whole.init();
         whole.start(c.rt);
-        if (!(!o.phases && !(o.all || o.ere))) c.round();
+        if (c.nf) {
+            if (c.opt.dump_level > 0) throw std::runtime_error("round dumps are not written for formula batches");
+            c.round_batch();
+        } else if (!(!o.phases && !(o.all || o.ere))) {
+            c.round();
+        }
         c.st.ms_total = whole.stop(c.rt);
         whole.destroy();
         if (c.opt.dump_level > 0) {
@@ -1160,6 +1446,7 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
 pf_status pf_sigma_result_sizes(pf_sigma_ctx* ctx, uint64_t* num_clauses, uint64_t* num_literals, uint64_t* num_units,
                                 uint64_t* num_resolved) {
     if (!ctx || !ctx->uploaded) return fail("no formula", PF_ESTATE);
+    if (ctx->nf) return fail("a formula batch: use pf_sigma_batch_result_sizes", PF_ESTATE);
     if (num_clauses) *num_clauses = ctx->ncls;
     if (num_literals) *num_literals = ctx->nlits_used;
     if (num_units) *num_units = ctx->ntrail;
@@ -1170,6 +1457,7 @@ pf_status pf_sigma_result_sizes(pf_sigma_ctx* ctx, uint64_t* num_clauses, uint64
 pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets, uint8_t* learnt, uint32_t* units,
                             uint32_t* resolved, uint8_t* eliminated) {
     if (!ctx || !ctx->uploaded) return fail("no formula", PF_ESTATE);
+    if (ctx->nf) return fail("a formula batch: use pf_sigma_batch_download", PF_ESTATE);
     return guarded([&]() -> pf_status {
         pf_sigma_ctx& c = *ctx;
         if (lits || offsets || learnt) {
@@ -1188,6 +1476,124 @@ pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets
         if (units && c.ntrail) c.rt.d2h(units, c.trail.p, (size_t)c.ntrail * 4);
         if (resolved && c.nresolved) c.rt.d2h(resolved, c.resolved.p, (size_t)c.nresolved * 4);
         if (eliminated) c.rt.d2h(eliminated, c.vstate.p, c.nvars + 1);
+        return PF_OK;
+    });
+}
+
+// ---------------------------------------------------------------- batch results
+// The store after a batched round holds every formula's surviving clauses in store
+// order; they are split per formula on the host, with literals back in each
+// formula's own numbering.
+struct BatchSplit {
+    std::vector<Hdr> H;
+    std::vector<u32> L, trail, resolved, fid_of_var;
+    std::vector<uint8_t> vstate;
+    std::vector<u32> cls_fid;                    // per clause
+    std::vector<std::array<u64, 3>> records;    // witness records: start, length, formula
+    std::vector<u64> ncl, nlit, nunit, nres;     // per formula
+};
+
+static void batch_split(pf_sigma_ctx& c, BatchSplit& b) {
+    const u32 nf = c.nf;
+    b.H = c.fetch(c.hdr.p, c.ncls);
+    b.L = c.fetch(c.lits.p, c.nlits_used);
+    b.trail = c.fetch(c.trail.p, c.ntrail);
+    b.resolved = c.fetch(c.resolved.p, c.nresolved);
+    b.fid_of_var = c.fetch(c.var_fid.p, c.nvars + 1);
+    b.vstate = c.fetch(c.vstate.p, c.nvars + 1);
+    b.ncl.assign(nf, 0);
+    b.nlit.assign(nf, 0);
+    b.nunit.assign(nf, 0);
+    b.nres.assign(nf, 0);
+    b.cls_fid.resize(c.ncls);
+    for (u32 i = 0; i < c.ncls; i++) {
+        const u32 f = b.fid_of_var[ABS(b.L[b.H[i].start])];
+        b.cls_fid[i] = f;
+        b.ncl[f]++;
+        b.nlit[f] += b.H[i].size;
+    }
+    for (u32 lit : b.trail) b.nunit[b.fid_of_var[ABS(lit)]]++;
+    b.records.clear();
+    for (u64 pos = b.resolved.size(); pos > 0;) {
+        const u64 len = b.resolved[pos - 1];
+        if (len == 0 || len + 1 > pos) throw std::runtime_error("malformed witness stack");
+        const u64 start = pos - 1 - len;
+        const u32 f = b.fid_of_var[ABS(b.resolved[start])];
+        b.records.push_back({start, len, f});
+        b.nres[f] += len + 1;
+        pos = start;
+    }
+    std::reverse(b.records.begin(), b.records.end());
+}
+
+pf_status pf_sigma_batch_result_sizes(pf_sigma_ctx* ctx, int32_t* status, uint32_t* phases, uint64_t* num_clauses,
+                                      uint64_t* num_literals, uint64_t* num_units, uint64_t* num_resolved) {
+    if (!ctx || !ctx->uploaded) return fail("no formula", PF_ESTATE);
+    if (!ctx->nf) return fail("not a formula batch", PF_ESTATE);
+    return guarded([&]() -> pf_status {
+        pf_sigma_ctx& c = *ctx;
+        BatchSplit b;
+        batch_split(c, b);
+        for (u32 f = 0; f < c.nf; f++) {
+            if (status) status[f] = c.f_status[f];
+            if (phases) phases[f] = c.f_phases[f];
+            if (num_clauses) num_clauses[f] = b.ncl[f];
+            if (num_literals) num_literals[f] = b.nlit[f];
+            if (num_units) num_units[f] = b.nunit[f];
+            if (num_resolved) num_resolved[f] = b.nres[f];
+        }
+        return PF_OK;
+    });
+}
+
+pf_status pf_sigma_batch_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets, uint8_t* learnt,
+                                  uint32_t* units, uint32_t* resolved, uint8_t* eliminated) {
+    if (!ctx || !ctx->uploaded) return fail("no formula", PF_ESTATE);
+    if (!ctx->nf) return fail("not a formula batch", PF_ESTATE);
+    return guarded([&]() -> pf_status {
+        pf_sigma_ctx& c = *ctx;
+        const u32 nf = c.nf;
+        BatchSplit b;
+        batch_split(c, b);
+        auto local = [&](u32 lit) { return lit - 2u * c.h_f_var[b.fid_of_var[ABS(lit)]]; };
+        // clauses: formula by formula, store order inside a formula
+        std::vector<u64> cbeg(nf + 1, 0), lbeg(nf + 1, 0);
+        for (u32 f = 0; f < nf; f++) {
+            cbeg[f + 1] = cbeg[f] + b.ncl[f];
+            lbeg[f + 1] = lbeg[f] + b.nlit[f];
+        }
+        std::vector<u64> cpos(cbeg.begin(), cbeg.end() - 1), lpos(lbeg.begin(), lbeg.end() - 1);
+        for (u32 i = 0; i < c.ncls; i++) {
+            const u32 f = b.cls_fid[i];
+            const Hdr& h = b.H[i];
+            const u64 k = cpos[f]++, o = lpos[f];
+            lpos[f] += h.size;
+            if (offsets) offsets[k] = o;
+            if (learnt) learnt[k] = h_learnt(h.flags) ? 1 : 0;
+            if (lits) for (u32 j = 0; j < h.size; j++) lits[o + j] = local(b.L[h.start + j]);
+        }
+        if (offsets) offsets[cbeg[nf]] = lbeg[nf];
+        if (units) {
+            std::vector<u64> ubeg(nf + 1, 0);
+            for (u32 f = 0; f < nf; f++) ubeg[f + 1] = ubeg[f] + b.nunit[f];
+            for (u32 lit : b.trail) units[ubeg[b.fid_of_var[ABS(lit)]]++] = local(lit);
+        }
+        if (resolved) {
+            std::vector<u64> rbeg(nf + 1, 0);
+            for (u32 f = 0; f < nf; f++) rbeg[f + 1] = rbeg[f] + b.nres[f];
+            for (const auto& r : b.records) {
+                u64& w = rbeg[r[2]];
+                for (u64 j = 0; j < r[1]; j++) resolved[w++] = local(b.resolved[r[0] + j]);
+                resolved[w++] = (u32)r[1];
+            }
+        }
+        if (eliminated) {
+            u64 w = 0;
+            for (u32 f = 0; f < nf; f++) {
+                eliminated[w++] = 0;
+                for (u32 v = c.h_f_var[f] + 1; v <= c.h_f_var[f] + c.h_f_nv[f]; v++) eliminated[w++] = b.vstate[v];
+            }
+        }
         return PF_OK;
     });
 }

@@ -58,6 +58,20 @@ def canonical(recs: list) -> dict:
     return res
 
 
+def canonical_result(status: int, res) -> dict:
+    """The form of ``canonical`` for a downloaded result (sigma.Result)."""
+    out = {"status": int(status)}
+    if out["status"] != 0:
+        return out
+    o = res.offsets.astype(np.int64)
+    cls = [(int(res.learnt[i]) & 1, tuple(int(x) for x in res.lits[o[i]:o[i + 1]])) for i in range(o.size - 1)]
+    out["clauses"] = sorted(cls)
+    out["resolved"] = res.resolved.tolist()
+    out["units"] = sorted(set(res.units.tolist()))
+    out["elim"] = [v for v in range(1, res.eliminated.size) if res.eliminated[v]]
+    return out
+
+
 def normalize(recs: list) -> list:
     """Mask what parallel unit propagation may legitimately change.
 

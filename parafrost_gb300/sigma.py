@@ -78,6 +78,14 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     lib.pf_sigma_download.restype = ctypes.c_int
     lib.pf_sigma_write_dump.argtypes = [_VP, ctypes.c_char_p]
     lib.pf_sigma_write_dump.restype = ctypes.c_int
+    lib.pf_sigma_upload_batch.argtypes = [_VP, _U32, _VP, _VP, _VP, _VP]
+    lib.pf_sigma_upload_batch.restype = ctypes.c_int
+    lib.pf_sigma_upload_batch_device.argtypes = [_VP, _U32, _VP, _VP, _VP, _VP]
+    lib.pf_sigma_upload_batch_device.restype = ctypes.c_int
+    lib.pf_sigma_batch_result_sizes.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
+    lib.pf_sigma_batch_result_sizes.restype = ctypes.c_int
+    lib.pf_sigma_batch_download.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
+    lib.pf_sigma_batch_download.restype = ctypes.c_int
     lib.pf_sigma_footprint.argtypes = [_VP, _VP]
     lib.pf_sigma_footprint.restype = ctypes.c_int
     lib.pf_sigma_destroy.argtypes = [_VP]
@@ -141,6 +149,25 @@ class Result:
         return [tuple(int(x) for x in self.lits[o[i]:o[i + 1]]) for i in range(o.size - 1)]
 
 
+def pack_batch(formulas):
+    """Concatenate (num_vars, lits, offsets) formulas: (num_vars[], lits, offsets)."""
+    nv = np.array([f[0] for f in formulas], dtype=np.uint32)
+    lits = np.concatenate([np.asarray(f[1], dtype=np.uint32) for f in formulas]) if formulas else np.empty(0, np.uint32)
+    parts, base = [np.zeros(1, dtype=np.uint64)], 0
+    for f in formulas:
+        o = np.asarray(f[2], dtype=np.uint64)
+        parts.append(o[1:] - o[0] + np.uint64(base))
+        base += int(o[-1] - o[0])
+    return nv, lits, np.concatenate(parts)
+
+
+def lits_offsets_begin(formulas, lits, offsets):
+    """clause_begin, lits, offsets of a packed batch."""
+    cb = np.zeros(len(formulas) + 1, dtype=np.uint64)
+    cb[1:] = np.cumsum([np.asarray(f[2]).size - 1 for f in formulas])
+    return cb, lits, offsets
+
+
 class Simplifier:
     """One resident formula on the current GPU (a pf_sigma_ctx)."""
 
@@ -193,6 +220,59 @@ class Simplifier:
         self._check(self.lib.pf_sigma_download(self.h, _ptr(lits), _ptr(offsets), _ptr(learnt), _ptr(units),
                                                _ptr(resolved), _ptr(elim)))
         return Result(self.num_vars, lits, offsets, learnt, units, resolved, elim)
+
+    # ---- formula batches
+    def awaken_batch(self, formulas) -> None:
+        """Upload a batch: formulas is a sequence of (num_vars, lits, offsets) in each
+        formula's own numbering."""
+        nv, lits, offs = pack_batch(formulas)
+        self.upload_batch(nv, *lits_offsets_begin(formulas, lits, offs))
+
+    def upload_batch(self, num_vars: np.ndarray, clause_begin: np.ndarray, lits: np.ndarray,
+                     offsets: np.ndarray) -> None:
+        num_vars = np.ascontiguousarray(num_vars, dtype=np.uint32)
+        clause_begin = np.ascontiguousarray(clause_begin, dtype=np.uint64)
+        lits = np.ascontiguousarray(lits, dtype=np.uint32)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        self._check(self.lib.pf_sigma_upload_batch(self.h, num_vars.size, _ptr(num_vars), _ptr(clause_begin),
+                                                   _ptr(lits), _ptr(offsets)))
+        self.batch_vars = num_vars.copy()
+
+    def upload_batch_device(self, num_vars: np.ndarray, clause_begin: np.ndarray, d_lits: int, d_offsets: int):
+        num_vars = np.ascontiguousarray(num_vars, dtype=np.uint32)
+        clause_begin = np.ascontiguousarray(clause_begin, dtype=np.uint64)
+        self._check(self.lib.pf_sigma_upload_batch_device(self.h, num_vars.size, _ptr(num_vars), _ptr(clause_begin),
+                                                          d_lits, d_offsets))
+        self.batch_vars = num_vars.copy()
+
+    def batch_results(self) -> list:
+        """[(status, phases, Result)] per formula of the last batched round."""
+        nf = self.batch_vars.size
+        st = np.empty(nf, dtype=np.int32)
+        ph = np.empty(nf, dtype=np.uint32)
+        nc, nl, nu, nr = (np.empty(nf, dtype=np.uint64) for _ in range(4))
+        self._check(self.lib.pf_sigma_batch_result_sizes(self.h, _ptr(st), _ptr(ph), _ptr(nc), _ptr(nl), _ptr(nu),
+                                                         _ptr(nr)))
+        C, Lt, U, R = int(nc.sum()), int(nl.sum()), int(nu.sum()), int(nr.sum())
+        lits = np.empty(Lt, dtype=np.uint32)
+        offsets = np.empty(C + 1, dtype=np.uint64)
+        learnt = np.empty(C, dtype=np.uint8)
+        units = np.empty(U, dtype=np.uint32)
+        resolved = np.empty(R, dtype=np.uint32)
+        elim = np.empty(int(self.batch_vars.astype(np.uint64).sum()) + nf, dtype=np.uint8)
+        self._check(self.lib.pf_sigma_batch_download(self.h, _ptr(lits), _ptr(offsets), _ptr(learnt), _ptr(units),
+                                                     _ptr(resolved), _ptr(elim)))
+        out = []
+        c0 = u0 = r0 = e0 = 0
+        for f in range(nf):
+            c1, u1, r1 = c0 + int(nc[f]), u0 + int(nu[f]), r0 + int(nr[f])
+            e1 = e0 + int(self.batch_vars[f]) + 1
+            o = offsets[c0:c1 + 1]
+            res = Result(int(self.batch_vars[f]), lits[int(o[0]):int(o[-1])].copy(), (o - o[0]).astype(np.uint64),
+                         learnt[c0:c1].copy(), units[u0:u1].copy(), resolved[r0:r1].copy(), elim[e0:e1].copy())
+            out.append((int(st[f]), int(ph[f]), res))
+            c0, u0, r0, e0 = c1, u1, r1, e1
+        return out
 
     def write_dump(self, path: str) -> None:
         self._check(self.lib.pf_sigma_write_dump(self.h, path.encode()))
