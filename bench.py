@@ -39,7 +39,13 @@ WORKLOADS = {
                           sample_kw=dict(num_vars=2_000_000, num_clauses=8_000_000, seed=1)),
     "ksat3-10k": dict(gen="random_ksat", kw=dict(num_vars=10_000, num_clauses=42_600, k=3, seed=1),
                       sample_kw=dict(num_vars=10_000, num_clauses=42_600, k=3, seed=1)),
+    # batched workload: 4096 random k-SAT formulas (k in 2..5 per clause), clause counts
+    # log-uniform in [1k, 200k], clause/variable ratio U[3.0, 4.5]; one batched round
+    # per step; unit formulas/s
+    "batch-4096": dict(gen="batch_ksat", kw=dict(num_formulas=4096, cmin=1_000, cmax=200_000, seed=1),
+                       sample_kw=dict(num_formulas=4096, cmin=1_000, cmax=200_000, seed=1), batch=True),
 }
+BATCH_UNIT = "CNFs/s"
 METRIC = "sigmify round ms & HBM GB/s; batched CNFs/s, p50/p99 latency vs plain GPU"
 UNIT = "clauses/s"
 
@@ -115,10 +121,61 @@ def cpu_round_seconds(nv, lits, off) -> tuple:
     return secs, "port"
 
 
+FORMULAS = None  # --formulas: a smaller batch of the same generator (quick runs)
+
+
+def batch_forms(name: str):
+    from parafrost_gb300 import cnfgen
+    kw = dict(WORKLOADS[name]["kw"])
+    if FORMULAS:
+        kw["num_formulas"] = FORMULAS
+    return list(cnfgen.batch_ksat(**kw))
+
+
+def _oracle_round_seconds(job):
+    """One formula through the reference CPU simplifier (a process-pool job)."""
+    nv, lits, off = job
+    return cpu_round_seconds(nv, lits, off)[0]
+
+
+def cpu_batch_rate(forms, sample: int, workers: int) -> tuple:
+    """Formulas/s of the CPU simplifier on `sample` formulas spread evenly over the
+    batch (every len/sample-th), `workers` processes, one formula per process at a
+    time: (rate, kind, description)."""
+    import multiprocessing as mp
+    from parafrost_gb300 import build
+    build.build_oracle()
+    import oracle_runner as orr
+    kind = "reference" if orr.reference_available() else "port"
+    step = max(1, len(forms) // sample)
+    jobs = forms[::step][:sample]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(workers) as pool:
+        pool.map(_oracle_round_seconds, jobs, chunksize=1)
+    secs = time.perf_counter() - t0
+    desc = (f"{len(jobs)} of the {len(forms)} formulas (every {step}th, "
+            f"{sum(j[2].size - 1 for j in jobs)} clauses), one round each, {workers} processes")
+    return len(jobs) / secs, kind, desc
+
+
 def run_reference(args) -> dict:
     rank, world, _ = dist_env()
     if rank != 0:
         return None
+    if WORKLOADS[args.workload].get("batch"):
+        forms = batch_forms(args.workload)
+        workers = max(1, os.cpu_count() or 1)
+        rates = []
+        for _ in range(args.warmup + args.steps):
+            rate, kind, desc = cpu_batch_rate(forms, max(workers, 16), workers)
+            rates.append(rate)
+        value = float(np.mean(rates[args.warmup:]))
+        return {"metric": METRIC, "value": value, "unit": BATCH_UNIT, "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * len(forms) / value,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic", "config": {"workload": args.workload, "sample": True},
+                "cpu_baseline": {"value": value, "unit": BATCH_UNIT, "cores": workers, "kind": kind, "sample": desc},
+                "e2e": {"value": value, "unit": BATCH_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     nv, lits, off = make_workload(args.workload, sample=True)
     ncls = off.size - 1
     for _ in range(args.warmup):
@@ -291,6 +348,150 @@ def run_ours(args) -> dict:
     return out if rank == 0 else None
 
 
+def run_ours_batch(args) -> dict:
+    """Batched workload: one batched round over all formulas per step (inputs
+    resident in device memory); e2e through the batch C ABI with host buffers."""
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from parafrost_gb300.options import Options
+    from parafrost_gb300.sigma import Simplifier, pack_batch, lits_offsets_begin
+
+    forms = batch_forms(args.workload)
+    # formulas are independent: rank r takes every world-th formula
+    forms = forms[rank::world]
+    nv, lits, off = pack_batch(forms)
+    cb, lits, off = lits_offsets_begin(forms, lits, off)
+    nf, ncls = len(forms), int(off.size - 1)
+    dev = torch.device("cuda", local)
+    d_lits = torch.from_numpy(lits.view(np.int32)).to(dev)
+    d_off = torch.from_numpy(off.view(np.int64)).to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    s = Simplifier(Options(all=1))
+
+    def step():
+        s.upload_batch_device(nv, cb, d_lits.data_ptr(), d_off.data_ptr())
+        return s.sigmify()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    for i in range(args.steps):
+        flush_l2(flush)
+        ev[i][0].record()
+        stats.append(step())
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    tot_ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
+    total_forms = nf
+    if world > 1:
+        t = torch.tensor([tot_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot_ms = float(t.item())
+        n = torch.tensor([nf], device=dev)
+        torch.distributed.all_reduce(n)
+        total_forms = int(n.item())
+    value = total_forms * args.steps / (tot_ms / 1e3)
+    last = stats[-1]
+    kern = {}
+    for k in last.as_dict()["kernels"]:
+        ms_k = float(np.sum([x.as_dict()["kernels"][k]["ms"] for x in stats]))
+        by_k = float(np.sum([x.as_dict()["kernels"][k]["bytes"] for x in stats]))
+        n_k = int(np.sum([x.as_dict()["kernels"][k]["launches"] for x in stats]))
+        kern[k] = {"ms_per_step": ms_k / args.steps, "launches_per_step": n_k / args.steps,
+                   "bytes_per_launch": by_k / max(n_k, 1), "ms_per_launch": ms_k / max(n_k, 1),
+                   "gbs": by_k / (ms_k / 1e3) / 1e9 if ms_k > 0 else None}
+    dom = max(kern, key=lambda k: kern[k]["ms_per_step"])
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = kern[dom]["gbs"] or 0.0
+
+    # e2e: host buffers through the batch C ABI (upload, round, per-formula download)
+    pin_l = torch.from_numpy(lits.view(np.int32)).pin_memory()
+    pin_o = torch.from_numpy(off.view(np.int64)).pin_memory()
+    hl, ho = pin_l.numpy().view(np.uint32), pin_o.numpy().view(np.uint64)
+    e2e_steps = 0 if args.no_e2e else 1
+    d2h = 0
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.upload_batch(nv, cb, hl, ho)
+        s.sigmify()
+        res = s.batch_results()
+        d2h = sum(r.lits.nbytes + r.offsets.nbytes + r.units.nbytes + r.resolved.nbytes + r.eliminated.nbytes
+                  for _, _, r in res)
+    e2e_s = (time.perf_counter() - t0) / max(e2e_steps, 1)
+    e2e_value = world * nf / e2e_s if e2e_steps else None
+    s.close()
+
+    # the same formulas one by one through the single-formula API (plain launches,
+    # one round per formula), on an evenly spread sample
+    seq = None
+    if not args.no_sequential:
+        step_k = max(1, nf // 128)
+        sample = forms[::step_k][:128]
+        one = Simplifier(Options(all=1))
+        dl = [(torch.from_numpy(np.asarray(l, dtype=np.uint32).view(np.int32)).to(dev),
+               torch.from_numpy(np.asarray(o, dtype=np.uint64).view(np.int64)).to(dev), v) for v, l, o in sample]
+        for dlits, doff, v in dl[:3]:  # warm-up
+            one.awaken_device(v, dlits.data_ptr(), doff.data_ptr(), doff.numel() - 1)
+            one.sigmify()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for dlits, doff, v in dl:
+            one.awaken_device(v, dlits.data_ptr(), doff.data_ptr(), doff.numel() - 1)
+            one.sigmify()
+        torch.cuda.synchronize()
+        seq = len(dl) / (time.perf_counter() - t0)
+        one.close()
+
+    out = {"metric": METRIC, "value": value, "unit": BATCH_UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
+           "scaling": "weak" if world > 1 else "strong", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+           "config": {"workload": args.workload, "formulas": total_forms, "clauses_rank0": ncls,
+                      "literals_rank0": int(lits.size), "options": "-all, phases=5",
+                      "l2": "inputs larger than L2; 256 MB flush between steps",
+                      "parallelism": f"formulas split over {world} ranks" if world > 1 else "one batched round"},
+           "round_ms": float(np.mean([x.ms_total for x in stats])),
+           "stage_ms": {k: float(np.mean([x.as_dict()["ms_stage"][k] for x in stats])) for k in last.as_dict()["ms_stage"]},
+           "result": {"clauses_after": int(last.clauses_after), "phases": int(last.phases_run),
+                      "launches_per_round": int(last.kernel_launches)},
+           "sequential_cnfs_per_s": seq,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": profiled_traffic(dom, args.workload), "kernel": dom,
+                        "algorithmic_bytes_per_launch": kern[dom]["bytes_per_launch"],
+                        "ms_per_launch": kern[dom]["ms_per_launch"],
+                        "peak_source": "MEASURED_PEAKS.json (hbm_gbs, of measured)" if peaks else "fallback"},
+           "kernels": kern,
+           "e2e": {"value": e2e_value, "unit": BATCH_UNIT, "h2d_bytes_per_step": int(lits.nbytes + off.nbytes),
+                   "d2h_bytes_per_step": int(d2h)},
+           "gpu_launches": int(np.sum([x.kernel_launches for x in stats])), "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        workers = max(1, os.cpu_count() or 1)
+        rate, kind, desc = cpu_batch_rate(batch_forms(args.workload), max(workers, 16), workers)
+        out["cpu_baseline"] = {"value": rate, "unit": BATCH_UNIT, "cores": workers, "kind": kind, "sample": desc}
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out if rank == 0 else None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -300,13 +501,17 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="aig-2.2m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-sequential", action="store_true", help="batched workload: skip the one-by-one comparison")
+    ap.add_argument("--formulas", type=int, default=None, help="batched workload: number of formulas")
     args = ap.parse_args()
+    global FORMULAS
+    FORMULAS = args.formulas
     if args.impl == "reference":
         out = run_reference(args)
     else:
         from parafrost_gb300 import build
         build.build_cuda()
-        out = run_ours(args)
+        out = run_ours_batch(args) if WORKLOADS[args.workload].get("batch") else run_ours(args)
     if out is not None:
         print(json.dumps(out))
 
