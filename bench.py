@@ -44,8 +44,12 @@ WORKLOADS = {
     # per step; unit formulas/s
     "batch-4096": dict(gen="batch_ksat", kw=dict(num_formulas=4096, cmin=1_000, cmax=200_000, seed=1),
                        sample_kw=dict(num_formulas=4096, cmin=1_000, cmax=200_000, seed=1), batch=True),
+    # serving: Poisson arrivals of unrolled-AIG requests (10k-5M clauses), rates swept
+    "serve-aig": dict(gen="serving_requests", kw=dict(num=32, seed=1), sample_kw=dict(num=32, seed=1), serve=True),
 }
 BATCH_UNIT = "CNFs/s"
+SERVE_UNIT = "req/s"
+SERVE_RATES = (100, 300, 1000, 3000, 5000)
 METRIC = "sigmify round ms & HBM GB/s; batched CNFs/s, p50/p99 latency vs plain GPU"
 UNIT = "clauses/s"
 
@@ -162,20 +166,25 @@ def run_reference(args) -> dict:
     rank, world, _ = dist_env()
     if rank != 0:
         return None
-    if WORKLOADS[args.workload].get("batch"):
-        forms = batch_forms(args.workload)
+    if WORKLOADS[args.workload].get("batch") or WORKLOADS[args.workload].get("serve"):
+        if WORKLOADS[args.workload].get("serve"):
+            from parafrost_gb300 import cnfgen
+            forms = cnfgen.serving_requests(**WORKLOADS[args.workload]["kw"])
+        else:
+            forms = batch_forms(args.workload)
+        unit = SERVE_UNIT if WORKLOADS[args.workload].get("serve") else BATCH_UNIT
         workers = max(1, os.cpu_count() or 1)
         rates = []
         for _ in range(args.warmup + args.steps):
             rate, kind, desc = cpu_batch_rate(forms, max(workers, 16), workers)
             rates.append(rate)
         value = float(np.mean(rates[args.warmup:]))
-        return {"metric": METRIC, "value": value, "unit": BATCH_UNIT, "impl": "reference", "n_gpus": args.gpus,
+        return {"metric": METRIC, "value": value, "unit": unit, "impl": "reference", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * len(forms) / value,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
                 "data": "synthetic", "config": {"workload": args.workload, "sample": True},
-                "cpu_baseline": {"value": value, "unit": BATCH_UNIT, "cores": workers, "kind": kind, "sample": desc},
-                "e2e": {"value": value, "unit": BATCH_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                "cpu_baseline": {"value": value, "unit": unit, "cores": workers, "kind": kind, "sample": desc},
+                "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     nv, lits, off = make_workload(args.workload, sample=True)
     ncls = off.size - 1
     for _ in range(args.warmup):
@@ -492,6 +501,51 @@ def run_ours_batch(args) -> dict:
     return out if rank == 0 else None
 
 
+def run_ours_serve(args) -> dict:
+    """Serving sweep: open-loop Poisson arrivals at each rate, batched server and
+    plain (one request per round) server; latency from arrival to result on host."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from parafrost_gb300 import cnfgen
+    from parafrost_gb300.options import Options
+    from parafrost_gb300.serve import Server, poisson_load, summarize
+
+    pool = cnfgen.serving_requests(**WORKLOADS[args.workload]["kw"])
+    per_rate = args.requests
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(free * 0.6)
+    sweep = []
+    clocks = Clocks(local)
+    clocks.start()
+    for mode in ("batched", "plain"):
+        with Server(Options(all=1), hbm_budget=budget, mode=mode) as srv:
+            poisson_load(srv, pool, rate=1000.0, num=max(args.warmup, 3), seed=99)  # warm-up
+        for rate in SERVE_RATES:
+            with Server(Options(all=1), hbm_budget=budget, mode=mode) as srv:
+                reqs = poisson_load(srv, pool, rate=float(rate), num=per_rate, seed=rate)
+            row = summarize(reqs, srv)
+            row.update(rate=rate, mode=mode)
+            sweep.append(row)
+            if mode == "plain" and row["p99_ms"] and row["p99_ms"] > 60_000:
+                break  # saturated far beyond the rate: higher rates only queue longer
+    clk = clocks.stop()
+    top = [r for r in sweep if r["mode"] == "batched"][-1]
+    value = top["formulas_per_s"]
+    return {"metric": METRIC, "value": value, "unit": SERVE_UNIT, "n_gpus": 1, "steps": per_rate,
+            "warmup": args.warmup, "ms_per_step": 1e3 / value if value else None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": args.workload, "pool": len(pool),
+                       "pool_clauses": int(sum(f[2].size - 1 for f in pool)), "requests_per_rate": per_rate,
+                       "rates": list(SERVE_RATES), "hbm_budget_bytes": budget,
+                       "timing": "wall clock from scheduled arrival to result on host"},
+            "sweep": sweep, "admitted_hbm_bytes": max(r["max_footprint_bytes"] for r in sweep),
+            "e2e": {"value": value, "unit": SERVE_UNIT,
+                    "h2d_bytes_per_step": int(np.mean([f[1].nbytes + f[2].nbytes for f in pool])),
+                    "d2h_bytes_per_step": None},
+            "gpu_launches": int(sum(r["gpu_launches"] for r in sweep)), "clocks": clk}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -503,6 +557,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-sequential", action="store_true", help="batched workload: skip the one-by-one comparison")
     ap.add_argument("--formulas", type=int, default=None, help="batched workload: number of formulas")
+    ap.add_argument("--requests", type=int, default=160, help="serving workload: requests per arrival rate")
     args = ap.parse_args()
     global FORMULAS
     FORMULAS = args.formulas
@@ -511,7 +566,12 @@ def main():
     else:
         from parafrost_gb300 import build
         build.build_cuda()
-        out = run_ours_batch(args) if WORKLOADS[args.workload].get("batch") else run_ours(args)
+        if WORKLOADS[args.workload].get("serve"):
+            out = run_ours_serve(args)
+        elif WORKLOADS[args.workload].get("batch"):
+            out = run_ours_batch(args)
+        else:
+            out = run_ours(args)
     if out is not None:
         print(json.dumps(out))
 

@@ -192,6 +192,86 @@ def aig_tseitin(num_inputs: int = 50_000, num_and: int = 2_000_000, num_xor: int
     return num_vars, out, off
 
 
+def aig_unrolled(num_gates: int = 5_000, steps: int = 5, num_inputs: int | None = None,
+                 num_latches: int | None = None, window: float = 0.10, seed: int = 1) -> tuple:
+    """Bounded unrolling of a seeded random sequential AIG (serving requests).
+
+    One frame has ``num_inputs`` inputs, ``num_latches`` latches and ``num_gates``
+    AND gates; gate fan-ins are two distinct earlier nodes of the frame (inputs,
+    latches, gates) from the most recent ``window`` fraction, with random
+    polarity. Frame 0's latches are fresh variables reset to 0 by unit clauses; frame
+    t's latches are the next-state literals (distinct gates, random polarity) of
+    frame t-1. Tseitin per gate: (-g a)(-g b)(g -a -b); the last frame asserts one
+    gate output (the property's bad state) as a unit clause.
+    """
+    ni = num_inputs if num_inputs is not None else max(2, num_gates // 10)
+    nl = num_latches if num_latches is not None else max(1, num_gates // 10)
+    nl = min(nl, num_gates)
+    st = Stream(seed, 7)
+    nodes = ni + nl + num_gates
+    g = np.arange(ni + nl + 1, nodes + 1, dtype=np.int64)  # gate node ids of a frame
+    lo = np.maximum(1, g - np.maximum(2, (window * (g - 1)).astype(np.int64)))
+    span = g - lo
+    next_var = 1
+    lits_parts, size_parts = [], []
+    latch_lits = None
+    for t in range(steps):
+        lit_of = np.zeros(nodes + 1, dtype=np.int64)
+        lit_of[1:ni + 1] = (np.arange(next_var, next_var + ni, dtype=np.int64) << 1)
+        next_var += ni
+        if t == 0:
+            lv = np.arange(next_var, next_var + nl, dtype=np.int64)
+            next_var += nl
+            lit_of[ni + 1:ni + nl + 1] = lv << 1
+            lits_parts.append(((lv << 1) | 1).astype(np.uint32))  # reset: latch = 0
+            size_parts.append(np.ones(nl, dtype=np.uint64))
+        else:
+            lit_of[ni + 1:ni + nl + 1] = latch_lits
+        gv = np.arange(next_var, next_var + num_gates, dtype=np.int64)
+        next_var += num_gates
+        lit_of[ni + nl + 1:] = gv << 1
+        a = lo + st.below(span, num_gates)
+        b = lo + st.below(span, num_gates)
+        while True:
+            same = np.nonzero(a == b)[0]
+            if same.size == 0:
+                break
+            b[same] = lo[same] + st.below(span[same], same.size)
+        la = lit_of[a] ^ st.below(2, num_gates)
+        lb = lit_of[b] ^ st.below(2, num_gates)
+        lg = gv << 1
+        blk = np.empty((num_gates, 7), dtype=np.int64)
+        blk[:, 0], blk[:, 1] = lg | 1, la
+        blk[:, 2], blk[:, 3] = lg | 1, lb
+        blk[:, 4], blk[:, 5], blk[:, 6] = lg, la ^ 1, lb ^ 1
+        lits_parts.append(blk.reshape(-1).astype(np.uint32))
+        size_parts.append(np.tile(np.array([2, 2, 3], dtype=np.uint64), num_gates))
+        # next-state literals: distinct gates of this frame
+        pick = np.argsort(st.u64(num_gates), kind="stable")[:nl]
+        latch_lits = (gv[pick] << 1) ^ st.below(2, nl)
+    bad = (int(next_var - 1 - st.below(num_gates, 1)[0]) << 1)
+    lits_parts.append(np.array([bad], dtype=np.uint32))
+    size_parts.append(np.ones(1, dtype=np.uint64))
+    off = np.concatenate([[0], np.cumsum(np.concatenate(size_parts))]).astype(np.uint64)
+    return next_var - 1, np.concatenate(lits_parts), off
+
+
+def serving_requests(num: int, seed: int = 1, cmin: int = 10_000, cmax: int = 5_000_000):
+    """Serving requests: unrolled AIGs with gates log-uniform in [5k, 50k] and steps
+    log-uniform in [5, 100], kept when the clause count is within [cmin, cmax]."""
+    st = Stream(seed, 8)
+    out, i = [], 0
+    while len(out) < num:
+        u = st.unit(2)
+        gates = int(np.exp(np.log(5_000) + u[0] * np.log(10.0)))
+        steps = int(np.exp(np.log(5) + u[1] * np.log(20.0)))
+        ncls = steps * 3 * gates + gates // 10 + 1
+        i += 1
+        if cmin <= ncls <= cmax:
+            out.append(aig_unrolled(gates, steps, seed=seed * 1_000_003 + i))
+    return out
+
+
 def community(num_vars: int = 20_000_000, num_clauses: int = 80_000_000, communities: int = 200,
               modularity: float = 0.8, mean_len: float = 3.5, max_len: int = 64,
               exponent: float = 2.5, seed: int = 1, chunk: int = 8_000_000, plant: bool = True) -> tuple:

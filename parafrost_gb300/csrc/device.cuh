@@ -284,4 +284,46 @@ enum : u32 {
     ERR_INPUT = 1u << 7,        // invalid input formula
 };
 
+#if SIGMA_CUDA
+// ---------------------------------------------------------------- grid barrier
+constexpr u64 kBarrierNs = 2000000000ull;  // a barrier wait longer than 2 s is an error
+
+DEV u64 global_ns() {
+    u64 t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Barrier over all blocks of a cooperative launch. A block whose wait runs out
+// records ERR_ITER and gets false (the launch then winds down).
+DEV bool grid_barrier(u32* bar, u32* err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const u32 gen = vload(&bar[1]);
+        __threadfence();
+        if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        } else {
+            const u64 t0 = global_ns();
+            while (vload(&bar[1]) == gen) {
+                if (global_ns() - t0 > kBarrierNs) {
+                    atomicOr(err, ERR_ITER);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+#endif
+
+
 }  // namespace sigma

@@ -30,52 +30,104 @@ struct PropArgs {
     u32 cap_work;
 };
 
+// Loads of data that earlier waves of the same launch may have written (the
+// persistent wave kernel): read at L2, past this SM's L1.
+template <bool Fresh, class T>
+HD T ldw(const T* p) {
+#if defined(__CUDA_ARCH__)
+    if (Fresh) return __ldcg(p);
+#endif
+    return *p;
+}
+template <bool Fresh>
+HD Hdr ldw_hdr(const Hdr* p) {
+#if defined(__CUDA_ARCH__)
+    if (Fresh) {
+        const uint4 v = __ldcg(reinterpret_cast<const uint4*>(p));
+        Hdr h;
+        h.start = v.x;
+        h.size = v.y;
+        h.sig = v.z;
+        h.flags = v.w;
+        return h;
+    }
+#endif
+    return *p;
+}
+
 // Wave A: one item per pending literal.
-HD void k_prop_lists(const PropArgs& a, u32 k) {
+template <bool Fresh>
+HD void prop_lists(const PropArgs& a, u32 k) {
     const Ctx& c = a.c;
-    const u32 t = c.trail[a.head + k];
+    const u32 t = ldw<Fresh>(&c.trail[a.head + k]);
     const u32 f = FLIP(t);
     // collect ot[-t]
-    const u32 fo = c.ot_off[f], fs = c.ot_size[f];
+    const u32 fo = c.ot_off[f], fs = ldw<Fresh>(&c.ot_size[f]);
     for (u32 i = 0; i < fs; i++) {
         const u32 r = c.ot_refs[fo + i];
-        if (h_deleted(c.hdr[r].flags)) continue;
-        if (atom_exch(&a.cl_stamp[r], a.stamp) == a.stamp) continue;
-        const u32 pos = atom_add(a.nwork, 1u);
+        const bool take = !h_deleted(ldw<Fresh>(&c.hdr[r].flags)) && atom_exch(&a.cl_stamp[r], a.stamp) != a.stamp;
+        const u32 pos = warp_append(a.nwork, take);  // one reservation per group of lanes
+        if (!take) continue;
         if (pos < a.cap_work) a.work[pos] = r;
         else set_err(c, ERR_CAP_SCRATCH);
     }
     // toblivion(ot[t])
-    const u32 to = c.ot_off[t], ts = c.ot_size[t];
+    const u32 to = c.ot_off[t], ts = ldw<Fresh>(&c.ot_size[t]);
     for (u32 i = 0; i < ts; i++) {
         const u32 r = c.ot_refs[to + i];
-        c.hdr[r].flags = (c.hdr[r].flags & ~3u) | ST_DELETED;
+        c.hdr[r].flags = (ldw<Fresh>(&c.hdr[r].flags) & ~3u) | ST_DELETED;
     }
     c.ot_size[t] = 0;
     c.ot_size[f] = 0;
 }
 
 // Wave B: one item per collected clause.
-HD void k_prop_clause(const PropArgs& a, u32 k) {
+constexpr u32 PROP_SHORT = 4;
+template <bool Fresh>
+HD void prop_clause(const PropArgs& a, u32 k) {
     const Ctx& c = a.c;
-    const u32 r = a.work[k];
-    Hdr h = c.hdr[r];
+    const u32 r = ldw<Fresh>(&a.work[k]);
+    Hdr h = ldw_hdr<Fresh>(&c.hdr[r]);
     if (h_deleted(h.flags)) return;
     u32* l = c.lits + h.start;
-    const u32 v0 = ABS(l[0]);  // names the formula if the clause empties
-    // satisfied?
-    for (u32 i = 0; i < h.size; i++) {
-        if (lit_value(c, l[i]) == 1) {
+    const u32 v0 = ABS(ldw<Fresh>(&l[0]));  // names the formula if the clause empties
+    u32 n = 0, sig = 0;
+    if (h.size <= PROP_SHORT) {
+        // short clause: all literals and their values loaded together
+        u32 L[PROP_SHORT];
+        int val[PROP_SHORT];
+#pragma unroll
+        for (u32 j = 0; j < PROP_SHORT; j++) L[j] = j < h.size ? ldw<Fresh>(&l[j]) : 0u;
+#pragma unroll
+        for (u32 j = 0; j < PROP_SHORT; j++) val[j] = j < h.size ? lit_value(c, L[j]) : 0;
+        bool sat = false;
+#pragma unroll
+        for (u32 j = 0; j < PROP_SHORT; j++) sat |= val[j] == 1;
+        if (sat) {
             c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
             return;
         }
-    }
-    u32 n = 0, sig = 0;
-    for (u32 i = 0; i < h.size; i++) {
-        const u32 lit = l[i];
-        if (lit_value(c, lit) == 0) continue;
-        l[n++] = lit;
-        sig |= MAPHASH(lit);
+#pragma unroll
+        for (u32 j = 0; j < PROP_SHORT; j++) {
+            if (j < h.size && val[j] != 0) {
+                l[n++] = L[j];
+                sig |= MAPHASH(L[j]);
+            }
+        }
+    } else {
+        // satisfied?
+        for (u32 i = 0; i < h.size; i++) {
+            if (lit_value(c, ldw<Fresh>(&l[i])) == 1) {
+                c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+                return;
+            }
+        }
+        for (u32 i = 0; i < h.size; i++) {
+            const u32 lit = ldw<Fresh>(&l[i]);
+            if (lit_value(c, lit) == 0) continue;
+            l[n++] = lit;
+            sig |= MAPHASH(lit);
+        }
     }
     h.size = n;
     h.sig = sig;
@@ -97,6 +149,86 @@ HD void k_prop_clause(const PropArgs& a, u32 k) {
         }
     }
 }
+
+HD void k_prop_lists(const PropArgs& a, u32 k) { prop_lists<false>(a, k); }
+
+#if SIGMA_CUDA
+// Wave A with one warp per pending literal (lanes take the list entries): used
+// when a wave has fewer literals than the launch has warps, where a thread walking
+// a whole list would be the wave's critical path.
+DEV void prop_lists_warp(const PropArgs& a, u32 k) {
+    const Ctx& c = a.c;
+    const u32 lane = threadIdx.x & 31u;
+    const u32 t = __ldcg(&c.trail[a.head + k]);
+    const u32 f = FLIP(t);
+    const u32 fo = c.ot_off[f], fs = __ldcg(&c.ot_size[f]);
+    const u32 to = c.ot_off[t], ts = __ldcg(&c.ot_size[t]);
+    for (u32 i = lane; i < fs; i += 32) {
+        const u32 r = c.ot_refs[fo + i];
+        const bool take = !h_deleted(__ldcg(&c.hdr[r].flags)) && atomicExch(&a.cl_stamp[r], a.stamp) != a.stamp;
+        const u32 pos = warp_append(a.nwork, take);
+        if (!take) continue;
+        if (pos < a.cap_work) a.work[pos] = r;
+        else set_err(c, ERR_CAP_SCRATCH);
+    }
+    for (u32 i = lane; i < ts; i += 32) {
+        const u32 r = c.ot_refs[to + i];
+        c.hdr[r].flags = (__ldcg(&c.hdr[r].flags) & ~3u) | ST_DELETED;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        c.ot_size[t] = 0;
+        c.ot_size[f] = 0;
+    }
+}
+#endif
+HD void k_prop_clause(const PropArgs& a, u32 k) { prop_clause<false>(a, k); }
+
+#if SIGMA_CUDA
+// Every wave of one propagation in one cooperative launch: wave A over the trail
+// literals [head, tail), a grid barrier, wave B over the collected clauses, a
+// barrier, then the literals wave B appended. Wave w uses work counter w & 1 and
+// clears the other one (last read in wave w-1, before its closing barrier).
+struct PropWaves {
+    u32* nwork2;     // two work counters
+    u32* bar;        // grid barrier words
+    u32* waves;      // out: waves run
+    u32 max_waves;
+};
+
+__global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
+    const u32 tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    u32 head = a.head;
+    for (u32 wave = 0;; wave++) {
+        const u32 tail = vload(a.c.ntrail);
+        if (tail == head) {
+            if (tid == 0) *w.waves = wave;
+            return;
+        }
+        if (wave >= w.max_waves) {
+            if (tid == 0) atomicOr(a.c.err, ERR_ITER);
+            return;
+        }
+        PropArgs b = a;
+        b.head = head;
+        b.stamp = a.stamp + wave;
+        b.nwork = &w.nwork2[wave & 1];
+        if (tid == 0) w.nwork2[(wave + 1) & 1] = 0;
+        const u32 nwarps = nth >> 5;
+        if (tail - head < nwarps) {
+            for (u32 i = tid >> 5; i < tail - head; i += nwarps) prop_lists_warp(b, i);
+        } else {
+            for (u32 i = tid; i < tail - head; i += nth) prop_lists<true>(b, i);
+        }
+        if (!grid_barrier(w.bar, a.c.err)) return;
+        const u32 n = vload(b.nwork);
+        const u32 nw = n < a.cap_work ? n : a.cap_work;
+        for (u32 i = tid; i < nw; i += nth) prop_clause<true>(b, i);
+        if (!grid_barrier(w.bar, a.c.err)) return;
+        head = tail;
+    }
+}
+#endif
 
 // reduceOT (src/cpu/simplify.cpp:58-79), run after propagation when SUB is off:
 // drop deleted clauses from every list.

@@ -117,6 +117,44 @@ struct FPvPartition {
     }
 };
 
+// Host split of a batch's trail and witness stack (kept from the sizes query to
+// the download; cleared by every upload and round).
+struct BatchSplit {
+    bool valid = false;
+    std::vector<u32> trail, resolved;
+    std::vector<std::array<u64, 3>> records;  // witness records: start, length, formula
+    std::vector<u64> nunit, nres;             // per formula
+};
+
+// Batch download: formula of every clause (key) with its index (value).
+struct FClauseFid {
+    Ctx c; u32* key; u32* val;
+    HD void operator()(u32 i) const {
+        key[i] = c.var_fid[ABS(c.lits[c.hdr[i].start])];
+        val[i] = i;
+    }
+};
+// Sizes and learnt flags in formula order.
+struct FClauseSize {
+    Ctx c; const u32* order; u64* size; uint8_t* learnt;
+    HD void operator()(u32 k) const {
+        const Hdr h = c.hdr[order[k]];
+        size[k] = h.size;
+        learnt[k] = h_learnt(h.flags) ? 1 : 0;
+    }
+};
+// Literals in formula order, in each formula's own numbering.
+struct FClauseGather {
+    Ctx c; const u32* order; const u32* fid; const u64* off; const u32* f_var; u32* out;
+    HD void operator()(u32 k) const {
+        const Hdr h = c.hdr[order[k]];
+        const u32 shift = 2u * f_var[fid[k]];
+        const u32* l = c.lits + h.start;
+        u32* o = out + off[k];
+        for (u32 j = 0; j < h.size; j++) o[j] = l[j] - shift;
+    }
+};
+
 enum Stage { ST_OT = 0, ST_PROP, ST_LCVE, ST_SORT, ST_SUB, ST_VE, ST_BCE, ST_ERE, ST_GC, ST_COUNT, ST_UP, ST_DOWN };
 
 }  // namespace
@@ -174,6 +212,7 @@ struct pf_sigma_ctx {
     DBuf<u64> f_count;  // [f] live clauses, [nf + f] live literals
     std::vector<int> f_status;
     std::vector<u32> f_phases;
+    BatchSplit split;
     // host state
     u32 npvs = 0;
     u32 n_go = 0;                  // elected variables of the formulas that go on (front of pvs)
@@ -241,17 +280,19 @@ struct pf_sigma_ctx {
     }
     void write_u32(u32* d, u32 v) { rt.h2d(d, &v, 4); }
 #if SIGMA_CUDA
-    // Blocks of the cooperative wave kernel: every block must be resident at once.
-    int waves_grid = 0;
-    int mis_waves_grid() {
-        if (!waves_grid) {
+    // Blocks of a cooperative wave kernel (256 threads): every block resident at once.
+    int mis_grid = 0;
+    template <class K>
+    int coop_grid(K kernel, int& cache) {
+        if (!cache) {
             int per_sm = 0;
-            ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mis_waves_k, 256, 0), "occupancy");
-            if (per_sm < 1) throw std::runtime_error("the wave kernel cannot be resident");
-            waves_grid = per_sm * rt.sms;
+            ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0), "occupancy");
+            if (per_sm < 1) throw std::runtime_error("a wave kernel cannot be resident");
+            cache = per_sm * rt.sms;
         }
-        return waves_grid;
+        return cache;
     }
+    int mis_waves_grid() { return coop_grid(mis_waves_k, mis_grid); }
 #endif
     void write_u64(u64* d, u64 v) { rt.h2d(d, &v, 8); }
 
@@ -381,6 +422,31 @@ struct pf_sigma_ctx {
             rt.zero(cl_stamp.p, cl_stamp.bytes());
             wave_stamp = 0;
         }
+#if SIGMA_CUDA
+        {
+            PropArgs a;
+            a.c = view();
+            a.head = prop_head;
+            a.stamp = wave_stamp + 1;
+            a.cl_stamp = cl_stamp.p;
+            a.work = work.p;
+            a.nwork = nullptr;
+            a.cap_work = (u32)work.n;
+            PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, nvars + 2};
+            rt.zero(counters.p + 22, 5 * 4);  // [22..23] work counters, [24..25] barrier, [26] waves
+            void* args[] = {&a, &w};
+            rt.launches++;
+            // four blocks per SM: most waves of a propagation are small, and the grid
+            // barrier between them costs one arrival per block
+            ck(cudaLaunchCooperativeKernel((const void*)prop_waves_k, dim3(rt.sms * 4), dim3(256), args, 0,
+                                           rt.stream),
+               "cooperative launch");
+            check();
+            wave_stamp += read_u32(counters.p + 26);
+            ntrail = read_u32(counters.p + 0);
+            prop_head = ntrail;
+        }
+#else
         u32 guard = 0;
         while (prop_head < ntrail) {
             if (++guard > nvars + 2) throw int(PF_ETIMEOUT);
@@ -401,6 +467,7 @@ struct pf_sigma_ctx {
             ntrail = read_u32(counters.p + 0);
             check();
         }
+#endif
         ot_dirty = true;
         if (!opt.sub) rt.each(FReduce{view()}, D);
     }
@@ -963,6 +1030,54 @@ struct pf_sigma_ctx {
         st.phases_run = phase;
     }
 
+    // Clauses of a batch's store grouped by formula (store order inside a formula,
+    // literals in the formula's numbering) straight into host buffers.
+    void batch_clauses_to(u32* h_lits, u64* h_off, uint8_t* h_learnt) {
+        const u32 n = ncls;
+        if (!n) {
+            if (h_off) h_off[0] = 0;
+            return;
+        }
+        big32a.reserve(rt, (size_t)n + 1);
+        big32b.reserve(rt, (size_t)n + 1);
+        work.reserve(rt, 2 * (size_t)n + 2);
+        radix_hist.reserve(rt, radix_hist_elems(n));
+        radix_hscan.reserve(rt, radix_hist_elems(n));
+        scan_tmp32.reserve(rt, scan_tmp_elems(radix_hist_elems(n)) + 4);
+        const Ctx c = view();
+        rt.each(FClauseFid{c, big32a.p, big32b.p}, n);
+        int bits = 8;
+        while (bits < 32 && (nf >> bits)) bits += 8;
+        radix_sort_pairs(big32a.p, big32b.p, work.p, work.p + n + 1, n, bits, radix_hist.p, radix_hscan.p,
+                         scan_tmp32.p, rt.stream);
+        rt.launches += 3 * (bits / 8);
+        big64a.reserve(rt, (size_t)n + 1);
+        big64b.reserve(rt, (size_t)n + 1);
+        DBuf<uint8_t> lrn;
+        lrn.reserve(rt, n);
+        rt.each(FClauseSize{c, big32b.p, big64a.p, lrn.p}, n);
+        const u64 total = scan64(big64a.p, big64b.p, n);
+        write_u64(big64b.p + n, total);
+        lits2.reserve(rt, (size_t)total + 1);
+        rt.each(FClauseGather{c, big32b.p, big32a.p, big64b.p, f_var.p, lits2.p}, n);
+        if (h_lits) rt.d2h(h_lits, lits2.p, (size_t)total * 4);
+        if (h_off) rt.d2h(h_off, big64b.p, ((size_t)n + 1) * 8);
+        if (h_learnt) rt.d2h(h_learnt, lrn.p, n);
+        lrn.free();
+    }
+
+    // Formula of a literal of the store, on the host.
+    u32 host_fid(u32 lit) const {
+        const u32 v = ABS(lit);
+        u32 lo = 0, hi = nf;
+        while (hi - lo > 1) {
+            const u32 mid = (lo + hi) >> 1;
+            if (h_f_var[mid] < v) lo = mid;
+            else hi = mid;
+        }
+        return lo;
+    }
+
     // ------------------------------------------------------------ formula batches
     // Each formula of a batch runs its own sigmifying loop; the formulas share the
     // store, so one phase does the stage kernels once for all formulas still in their
@@ -1227,6 +1342,9 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         c.nvars = num_vars;
         c.D = 2 * (num_vars + 1);
         c.nf = batch ? batch->nf : 0u;
+        c.split = BatchSplit();
+        c.fc_cls.clear();
+        c.fc_lits.clear();
         c.ncls = (u32)num_clauses;
         c.nlits_used = L;
         c.ntrail = c.prop_head = 0;
@@ -1380,6 +1498,7 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     c.alg_bytes = 0;
     c.mis_rounds = 0;
     c.rt.launches = 0;
+    c.split = BatchSplit();
     for (int k = 0; k < pf_sigma_ctx::K_COUNT; k++) {
         c.kclock[k].reset();
         c.kbytes[k] = 0;
@@ -1481,49 +1600,29 @@ pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets
 }
 
 // ---------------------------------------------------------------- batch results
-// The store after a batched round holds every formula's surviving clauses in store
-// order; they are split per formula on the host, with literals back in each
-// formula's own numbering.
-struct BatchSplit {
-    std::vector<Hdr> H;
-    std::vector<u32> L, trail, resolved, fid_of_var;
-    std::vector<uint8_t> vstate;
-    std::vector<u32> cls_fid;                    // per clause
-    std::vector<std::array<u64, 3>> records;    // witness records: start, length, formula
-    std::vector<u64> ncl, nlit, nunit, nres;     // per formula
-};
-
+// Clauses are grouped per formula on the device (a stable sort of the store by
+// formula); the trail and the witness stack are split on the host, with literals
+// back in each formula's own numbering.
 static void batch_split(pf_sigma_ctx& c, BatchSplit& b) {
     const u32 nf = c.nf;
-    b.H = c.fetch(c.hdr.p, c.ncls);
-    b.L = c.fetch(c.lits.p, c.nlits_used);
+    if (b.valid) return;
     b.trail = c.fetch(c.trail.p, c.ntrail);
     b.resolved = c.fetch(c.resolved.p, c.nresolved);
-    b.fid_of_var = c.fetch(c.var_fid.p, c.nvars + 1);
-    b.vstate = c.fetch(c.vstate.p, c.nvars + 1);
-    b.ncl.assign(nf, 0);
-    b.nlit.assign(nf, 0);
     b.nunit.assign(nf, 0);
     b.nres.assign(nf, 0);
-    b.cls_fid.resize(c.ncls);
-    for (u32 i = 0; i < c.ncls; i++) {
-        const u32 f = b.fid_of_var[ABS(b.L[b.H[i].start])];
-        b.cls_fid[i] = f;
-        b.ncl[f]++;
-        b.nlit[f] += b.H[i].size;
-    }
-    for (u32 lit : b.trail) b.nunit[b.fid_of_var[ABS(lit)]]++;
+    for (u32 lit : b.trail) b.nunit[c.host_fid(lit)]++;
     b.records.clear();
     for (u64 pos = b.resolved.size(); pos > 0;) {
         const u64 len = b.resolved[pos - 1];
         if (len == 0 || len + 1 > pos) throw std::runtime_error("malformed witness stack");
         const u64 start = pos - 1 - len;
-        const u32 f = b.fid_of_var[ABS(b.resolved[start])];
+        const u32 f = c.host_fid(b.resolved[start]);
         b.records.push_back({start, len, f});
         b.nres[f] += len + 1;
         pos = start;
     }
     std::reverse(b.records.begin(), b.records.end());
+    b.valid = true;
 }
 
 pf_status pf_sigma_batch_result_sizes(pf_sigma_ctx* ctx, int32_t* status, uint32_t* phases, uint64_t* num_clauses,
@@ -1532,13 +1631,14 @@ pf_status pf_sigma_batch_result_sizes(pf_sigma_ctx* ctx, int32_t* status, uint32
     if (!ctx->nf) return fail("not a formula batch", PF_ESTATE);
     return guarded([&]() -> pf_status {
         pf_sigma_ctx& c = *ctx;
-        BatchSplit b;
-        batch_split(c, b);
+        if (c.fc_cls.size() != c.nf) c.count_formulas();
+        BatchSplit& b = c.split;
+        if (num_units || num_resolved) batch_split(c, b);
         for (u32 f = 0; f < c.nf; f++) {
             if (status) status[f] = c.f_status[f];
             if (phases) phases[f] = c.f_phases[f];
-            if (num_clauses) num_clauses[f] = b.ncl[f];
-            if (num_literals) num_literals[f] = b.nlit[f];
+            if (num_clauses) num_clauses[f] = c.fc_cls[f];
+            if (num_literals) num_literals[f] = c.fc_lits[f];
             if (num_units) num_units[f] = b.nunit[f];
             if (num_resolved) num_resolved[f] = b.nres[f];
         }
@@ -1553,45 +1653,36 @@ pf_status pf_sigma_batch_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* o
     return guarded([&]() -> pf_status {
         pf_sigma_ctx& c = *ctx;
         const u32 nf = c.nf;
-        BatchSplit b;
-        batch_split(c, b);
-        auto local = [&](u32 lit) { return lit - 2u * c.h_f_var[b.fid_of_var[ABS(lit)]]; };
-        // clauses: formula by formula, store order inside a formula
-        std::vector<u64> cbeg(nf + 1, 0), lbeg(nf + 1, 0);
-        for (u32 f = 0; f < nf; f++) {
-            cbeg[f + 1] = cbeg[f] + b.ncl[f];
-            lbeg[f + 1] = lbeg[f] + b.nlit[f];
-        }
-        std::vector<u64> cpos(cbeg.begin(), cbeg.end() - 1), lpos(lbeg.begin(), lbeg.end() - 1);
-        for (u32 i = 0; i < c.ncls; i++) {
-            const u32 f = b.cls_fid[i];
-            const Hdr& h = b.H[i];
-            const u64 k = cpos[f]++, o = lpos[f];
-            lpos[f] += h.size;
-            if (offsets) offsets[k] = o;
-            if (learnt) learnt[k] = h_learnt(h.flags) ? 1 : 0;
-            if (lits) for (u32 j = 0; j < h.size; j++) lits[o + j] = local(b.L[h.start + j]);
-        }
-        if (offsets) offsets[cbeg[nf]] = lbeg[nf];
-        if (units) {
-            std::vector<u64> ubeg(nf + 1, 0);
-            for (u32 f = 0; f < nf; f++) ubeg[f + 1] = ubeg[f] + b.nunit[f];
-            for (u32 lit : b.trail) units[ubeg[b.fid_of_var[ABS(lit)]]++] = local(lit);
-        }
-        if (resolved) {
-            std::vector<u64> rbeg(nf + 1, 0);
-            for (u32 f = 0; f < nf; f++) rbeg[f + 1] = rbeg[f] + b.nres[f];
-            for (const auto& r : b.records) {
-                u64& w = rbeg[r[2]];
-                for (u64 j = 0; j < r[1]; j++) resolved[w++] = local(b.resolved[r[0] + j]);
-                resolved[w++] = (u32)r[1];
+        if (lits || offsets || learnt) c.batch_clauses_to(lits, offsets, learnt);
+        auto local = [&](u32 lit, u32 f) { return lit - 2u * c.h_f_var[f]; };
+        if (units || resolved) {
+            BatchSplit& b = c.split;
+            batch_split(c, b);
+            if (units) {
+                std::vector<u64> ubeg(nf + 1, 0);
+                for (u32 f = 0; f < nf; f++) ubeg[f + 1] = ubeg[f] + b.nunit[f];
+                for (u32 lit : b.trail) {
+                    const u32 f = c.host_fid(lit);
+                    units[ubeg[f]++] = local(lit, f);
+                }
+            }
+            if (resolved) {
+                std::vector<u64> rbeg(nf + 1, 0);
+                for (u32 f = 0; f < nf; f++) rbeg[f + 1] = rbeg[f] + b.nres[f];
+                for (const auto& r : b.records) {
+                    u64& w = rbeg[r[2]];
+                    for (u64 j = 0; j < r[1]; j++) resolved[w++] = local(b.resolved[r[0] + j], (u32)r[2]);
+                    resolved[w++] = (u32)r[1];
+                }
             }
         }
         if (eliminated) {
+            const std::vector<uint8_t> vs = c.fetch(c.vstate.p, c.nvars + 1);
             u64 w = 0;
             for (u32 f = 0; f < nf; f++) {
                 eliminated[w++] = 0;
-                for (u32 v = c.h_f_var[f] + 1; v <= c.h_f_var[f] + c.h_f_nv[f]; v++) eliminated[w++] = b.vstate[v];
+                std::memcpy(eliminated + w, vs.data() + c.h_f_var[f] + 1, c.h_f_nv[f]);
+                w += c.h_f_nv[f];
             }
         }
         return PF_OK;

@@ -1,0 +1,227 @@
+"""Serving loop: simplification requests arrive over time and are answered by
+batched sigmify rounds on one GPU.
+
+A request is one formula. The server thread takes every request that is waiting
+when the GPU becomes free, admits them in arrival order while their estimated
+device footprint fits the HBM budget (and the batch's formula cap), and runs one
+batched round over them (``pf_sigma_upload_batch`` -> ``pf_sigma_round`` ->
+``pf_sigma_batch_download``): each formula gets exactly the result of its own
+round. In ``plain`` mode every request runs alone through the single-formula
+calls instead, the comparison point for batching. Latency is measured from a
+request's arrival to the moment its result is on the host.
+
+There is no counterpart in the reference (ParaFROST simplifies the formula of one
+solver object inside ``sigmify()``); the per-formula work is the reference's
+round, unchanged.
+"""
+from __future__ import annotations
+
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .options import Options
+from .sigma import Result, Simplifier, pack_batch, lits_offsets_begin
+
+
+def estimate_footprint(num_vars: int, num_clauses: int, num_literals: int) -> int:
+    """Device bytes a formula needs inside a context: clause store with growth room
+    (headers 16 B + stamps 4 B per clause slot, 1.5x), literals and occurrence refs
+    (4 B each, 1.5x), witness room (4 B per literal + 8 B per variable), about 110 B
+    of per-variable arrays, and a third more for stage scratch."""
+    b = 1.5 * 20 * num_clauses + 1.5 * 8 * num_literals + 4 * num_literals + 118 * num_vars
+    return int(b * 4 / 3) + 4096
+
+
+@dataclass
+class Request:
+    formula: tuple                # (num_vars, lits, offsets)
+    arrival: float                # time.perf_counter() when it arrived
+    done: threading.Event = field(default_factory=threading.Event)
+    status: int | None = None     # PF_OK / PF_UNSAT, or a negative pf_status
+    phases: int = 0
+    result: Result | None = None
+    error: str | None = None
+    finished: float = 0.0
+    batch: int = -1               # index of the batch that served it
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+    def wait(self, timeout: float | None = None) -> bool:
+        return self.done.wait(timeout)
+
+
+class Server:
+    """One GPU, one server thread, requests answered in arrival order."""
+
+    def __init__(self, opts: Options | None = None, hbm_budget: int = 64 << 30, max_batch: int = 4096,
+                 mode: str = "batched", library: str | None = None):
+        if mode not in ("batched", "plain"):
+            raise ValueError("mode is 'batched' or 'plain'")
+        self.opts = opts or Options(all=1)
+        self.hbm_budget = int(hbm_budget)
+        self.max_batch = int(max_batch)
+        self.mode = mode
+        self.library = library
+        self.q: queue.Queue = queue.Queue()
+        self.batches: list = []          # (formulas, clauses, estimated bytes, device bytes held after, launches)
+        self._launches = 0
+        self.max_footprint = 0
+        self._stop = threading.Event()
+        self._thread: threading.Thread | None = None
+        self._pending: list = []
+
+    # ---- client side
+    def submit(self, formula: tuple, arrival: float | None = None) -> Request:
+        r = Request(formula, time.perf_counter() if arrival is None else arrival)
+        nv, lits, off = formula
+        if estimate_footprint(nv, off.size - 1, lits.size) > self.hbm_budget:
+            self._finish(r, -2, error="request larger than the HBM budget")
+            return r
+        self.q.put(r)
+        return r
+
+    def start(self) -> "Server":
+        self._thread = threading.Thread(target=self._run, name="sigma-server", daemon=True)
+        self._thread.start()
+        return self
+
+    def stop(self, timeout: float | None = None) -> None:
+        self._stop.set()
+        self.q.put(None)
+        if self._thread:
+            self._thread.join(timeout)
+
+    def __enter__(self):
+        return self.start()
+
+    def __exit__(self, *exc):
+        self.stop()
+
+    # ---- server side
+    def _finish(self, r: Request, status: int, phases: int = 0, result=None, error=None, batch: int = -1):
+        r.status, r.phases, r.result, r.error, r.batch = status, phases, result, error, batch
+        r.finished = time.perf_counter()
+        r.done.set()
+
+    def _admit(self) -> list:
+        """The next batch: waiting requests in arrival order while they fit."""
+        reqs = self._pending
+        self._pending = []
+        if not reqs:
+            first = self.q.get()
+            if first is None:
+                return []
+            reqs = [first]
+        while True:
+            try:
+                r = self.q.get_nowait()
+            except queue.Empty:
+                break
+            if r is None:
+                self._stop.set()
+                break
+            reqs.append(r)
+        batch, used = [], 0
+        for i, r in enumerate(reqs):
+            nv, lits, off = r.formula
+            need = estimate_footprint(nv, off.size - 1, lits.size)
+            if batch and (used + need > self.hbm_budget or len(batch) >= self.max_batch):
+                self._pending = reqs[i:]
+                break
+            batch.append(r)
+            used += need
+        return batch
+
+    def _run(self) -> None:
+        ctx = Simplifier(self.opts, library=self.library)
+        try:
+            while True:
+                if self._stop.is_set() and not self._pending and self.q.empty():
+                    break
+                batch = self._admit()
+                if not batch:
+                    if self._stop.is_set():
+                        break
+                    continue
+                bi = len(self.batches)
+                self._launches = 0
+                if self.mode == "plain":
+                    for r in batch:
+                        self._serve_one(ctx, r, bi)
+                else:
+                    self._serve_batch(ctx, batch, bi)
+                fp = ctx.footprint()
+                self.max_footprint = max(self.max_footprint, fp)
+                est = sum(estimate_footprint(r.formula[0], r.formula[2].size - 1, r.formula[1].size) for r in batch)
+                self.batches.append((len(batch), int(sum(r.formula[2].size - 1 for r in batch)), est, fp,
+                                     self._launches))
+        finally:
+            ctx.close()
+
+    def _serve_one(self, ctx: Simplifier, r: Request, bi: int) -> None:
+        nv, lits, off = r.formula
+        try:
+            ctx.awaken(nv, lits, off)
+            st = ctx.sigmify()
+            self._launches += st.kernel_launches
+            self._finish(r, st.status, st.phases_run, ctx.result() if st.status == 0 else None, batch=bi)
+        except Exception as e:  # the request fails, the server goes on
+            self._finish(r, getattr(e, "status", -4), error=str(e), batch=bi)
+
+    def _serve_batch(self, ctx: Simplifier, batch: list, bi: int) -> None:
+        forms = [r.formula for r in batch]
+        try:
+            nv, lits, off = pack_batch(forms)
+            cb, lits, off = lits_offsets_begin(forms, lits, off)
+            ctx.upload_batch(nv, cb, lits, off)
+            st = ctx.sigmify()
+            self._launches += st.kernel_launches
+            out = ctx.batch_results()
+        except Exception as e:
+            for r in batch:
+                self._finish(r, getattr(e, "status", -4), error=str(e), batch=bi)
+            return
+        for r, (st, ph, res) in zip(batch, out):
+            self._finish(r, st, ph, res if st == 0 else None, batch=bi)
+
+
+def poisson_load(server: Server, pool: list, rate: float, num: int, seed: int = 1) -> list:
+    """Open-loop Poisson arrivals at `rate` requests/s: request i (formula
+    pool[i % len(pool)]) is submitted at its scheduled time, which is also its
+    arrival time (a late submit does not hide queueing). Returns the requests after
+    all have finished."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=num)
+    t0 = time.perf_counter()
+    sched = t0 + np.cumsum(gaps)
+    reqs = []
+    for i in range(num):
+        delay = sched[i] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        reqs.append(server.submit(pool[i % len(pool)], arrival=float(sched[i])))
+    for r in reqs:
+        r.wait()
+    return reqs
+
+
+def summarize(reqs: list, server: Server) -> dict:
+    lat = np.array([r.latency for r in reqs if r.status is not None and r.status >= 0])
+    first = min(r.arrival for r in reqs)
+    last = max(r.finished for r in reqs)
+    ok = [r for r in reqs if r.status is not None and r.status >= 0]
+    return {"requests": len(reqs), "served": len(ok), "failed": len(reqs) - len(ok),
+            "formulas_per_s": len(ok) / (last - first) if last > first else None,
+            "clauses_per_s": sum(r.formula[2].size - 1 for r in ok) / (last - first) if last > first else None,
+            "p50_ms": float(np.percentile(lat, 50) * 1e3) if lat.size else None,
+            "p99_ms": float(np.percentile(lat, 99) * 1e3) if lat.size else None,
+            "batches": len(server.batches),
+            "mean_batch": float(np.mean([b[0] for b in server.batches])) if server.batches else 0.0,
+            "gpu_launches": int(sum(b[4] for b in server.batches)),
+            "max_footprint_bytes": int(server.max_footprint)}

@@ -268,8 +268,8 @@ class Simplifier:
             c1, u1, r1 = c0 + int(nc[f]), u0 + int(nu[f]), r0 + int(nr[f])
             e1 = e0 + int(self.batch_vars[f]) + 1
             o = offsets[c0:c1 + 1]
-            res = Result(int(self.batch_vars[f]), lits[int(o[0]):int(o[-1])].copy(), (o - o[0]).astype(np.uint64),
-                         learnt[c0:c1].copy(), units[u0:u1].copy(), resolved[r0:r1].copy(), elim[e0:e1].copy())
+            res = Result(int(self.batch_vars[f]), lits[int(o[0]):int(o[-1])], o - o[0],
+                         learnt[c0:c1], units[u0:u1], resolved[r0:r1], elim[e0:e1])
             out.append((int(st[f]), int(ph[f]), res))
             c0, u0, r0, e0 = c1, u1, r1, e1
         return out
