@@ -370,8 +370,9 @@ def run_ours_batch(args) -> dict:
     from parafrost_gb300.sigma import Simplifier, pack_batch, lits_offsets_begin
 
     forms = batch_forms(args.workload)
-    # formulas are independent: rank r takes every world-th formula
-    forms = forms[rank::world]
+    # formulas are independent: each rank takes a footprint-balanced share
+    from parafrost_gb300.shard import shard_formulas
+    forms = [forms[i] for i in shard_formulas(forms, world)[rank]]
     nv, lits, off = pack_batch(forms)
     cb, lits, off = lits_offsets_begin(forms, lits, off)
     nf, ncls = len(forms), int(off.size - 1)
