@@ -112,8 +112,7 @@ constexpr u32 MIS_CHUNK = 4;
 
 // Occurrences of graph vertices ranked below rv (other than v) in clause r, and
 // the clause's bytes (8 + 4*len when live) added to ws.
-HD u32 mis_lower_in_clause(const LcveArgs& a, u32 v, u32 rv, u32 r, u64& ws) {
-    const Hdr h = hdr_ro(&a.c.hdr[r]);
+HD u32 mis_lower_in_hdr(const LcveArgs& a, u32 v, u32 rv, const Hdr& h, u64& ws) {
     if (h_deleted(h.flags)) return 0;
     ws += 8ull + 4ull * h.size;
     const u32* L = a.c.lits + h.start;
@@ -127,6 +126,9 @@ HD u32 mis_lower_in_clause(const LcveArgs& a, u32 v, u32 rv, u32 r, u64& ws) {
     }
     return n;
 }
+HD u32 mis_lower_in_clause(const LcveArgs& a, u32 v, u32 rv, u32 r, u64& ws) {
+    return mis_lower_in_hdr(a, v, rv, hdr_ro(&a.c.hdr[r]), ws);
+}
 
 // Stores the lower-neighbour count of graph vertex v; a vertex with none goes in
 // and is returned true (the caller puts it on the first frontier).
@@ -139,13 +141,22 @@ HD bool mis_set_count(const LcveArgs& a, u32 v, u32 rv, u32 n) {
     return n == 0;
 }
 
+// The next clause's header is loaded before the current clause's literals are
+// examined, so two clause walks overlap.
 HD bool mis_count_one(const LcveArgs& a, u32 v, u64& ws) {
     const u32 rv = mis_rank(a.word[v]);
+    const u32 p = V2L(v), np = a.c.ot_size[p], n_all = np + a.c.ot_size[p + 1];
+    const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
+    ws += 4ull * n_all;
     u32 n = 0;
-    for (u32 side = 0; side < 2; side++) {
-        const u32 l = V2L(v) + side, o = a.c.ot_off[l], s = a.c.ot_size[l];
-        ws += 4ull * s;
-        for (u32 i = 0; i < s; i++) n += mis_lower_in_clause(a, v, rv, ldro(&a.c.ot_refs[o + i]), ws);
+    if (n_all) {
+        Hdr h = hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[op])]);
+        for (u32 t = 0; t < n_all; t++) {
+            Hdr hn = h;
+            if (t + 1 < n_all) hn = hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1])]);
+            n += mis_lower_in_hdr(a, v, rv, h, ws);
+            h = hn;
+        }
     }
     return mis_set_count(a, v, rv, n);
 }

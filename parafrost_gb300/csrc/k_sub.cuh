@@ -327,25 +327,32 @@ struct SubReachArgs {
     u32* npairs;
     u32 cap_pairs;
 };
-HD void k_sub_reach(const SubReachArgs& a, u32 q) {
+// One item per (unit, clause of the unit's list): a unit's list can be long (hub
+// variables), so its clauses are spread over threads. item_off is the exclusive
+// scan of the units' list sizes.
+HD void k_sub_reach(const SubReachArgs& a, const u32* item_off, u32 nunits, u32 item) {
     const Ctx& c = a.c;
+    u32 lo = 0, hi = nunits;  // unit q: item_off[q] <= item < item_off[q+1]
+    while (hi - lo > 1) {
+        const u32 mid = (lo + hi) >> 1;
+        if (item_off[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    const u32 q = lo;
     const U2 u = a.units[q];
-    const u32 lit = u.y;
-    const u32 o = c.ot_off[lit], s = c.ot_size[lit];
-    for (u32 i = 0; i < s; i++) {
-        const Hdr h = c.hdr[c.ot_refs[o + i]];
-        const u32* l = c.lits + h.start;
-        for (u32 t = 0; t < h.size; t++) {
-            const u32 owner = c.pvrank[ABS(l[t])];
-            if (owner != NONE && owner > u.x) {
-                const u32 pos = atom_add(a.npairs, 1u);
-                if (pos < a.cap_pairs) a.pairs[pos] = mk_u2(owner, q);
-                else set_err(c, ERR_CAP_SCRATCH);
-                break;
-            }
+    const Hdr h = c.hdr[c.ot_refs[c.ot_off[u.y] + (item - item_off[q])]];
+    const u32* l = c.lits + h.start;
+    for (u32 t = 0; t < h.size; t++) {
+        const u32 owner = c.pvrank[ABS(l[t])];
+        if (owner != NONE && owner > u.x) {
+            const u32 pos = atom_add(a.npairs, 1u);
+            if (pos < a.cap_pairs) a.pairs[pos] = mk_u2(owner, q);
+            else set_err(c, ERR_CAP_SCRATCH);
+            break;
         }
     }
 }
+HD void k_sub_reach_size(const Ctx& c, const U2* units, u32* size, u32 q) { size[q] = c.ot_size[units[q].y]; }
 
 // Commit of one unit: delete every clause of ot[lit] and empty the list.
 HD void k_sub_commit_oblivion(const Ctx& c, const u32* lits_, u32 q) {

@@ -59,8 +59,10 @@ struct FSubPv { SubArgs a; HD void operator()(u32 i) const { k_sub_pv(a, i); } }
 struct FSubNeed { Ctx c; const u32* pvs; u32* ent; u64* words; HD void operator()(u32 i) const { k_sub_need(c, pvs, ent, words, i); } };
 struct FSubSave { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_save(a, i); } };
 struct FSubRestore { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_restore(a, i); } };
-struct FSubReach { SubReachArgs a; HD void operator()(u32 i) const { k_sub_reach(a, i); } };
+struct FSubReach { SubReachArgs a; const u32* off; u32 nq; HD void operator()(u32 i) const { k_sub_reach(a, off, nq, i); } };
+struct FSubReachSize { Ctx c; const U2* units; u32* size; HD void operator()(u32 q) const { k_sub_reach_size(c, units, size, q); } };
 struct FSubCommit { Ctx c; const u32* lits; HD void operator()(u32 i) const { k_sub_commit_oblivion(c, lits, i); } };
+struct FSubAssign { Ctx c; const U2* units; HD void operator()(u32 i) const { enqueue_unit(c, units[i].y); } };
 struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) const { k_bve_scratch_need(c, pvs, need, i); } };
 struct FBveAnalyze { BveArgs a; HD void operator()(u32 i) const { bve_analyze_one(a, i, nullptr); } };
 struct FBveAnalyzeStaged { BveArgs a; HD void operator()(u32 i) const { k_bve_analyze(a, i); } };
@@ -664,7 +666,12 @@ struct pf_sigma_ctx {
             sub_pairs.reserve(rt, cap_pairs);
             write_u32(counters.p + 6, 0);
             SubReachArgs ra{view(), sub_units.p, sub_pairs.p, counters.p + 6, (u32)cap_pairs};
-            rt.each(FSubReach{ra}, (u32)units.size());
+            const u32 nq = (u32)units.size();
+            big32a.reserve(rt, (size_t)nq + 1);
+            big32b.reserve(rt, (size_t)nq + 1);
+            rt.each(FSubReachSize{view(), sub_units.p, big32a.p}, nq);
+            const u32 items = scan32(big32a.p, big32b.p, nq);
+            rt.each(FSubReach{ra, big32b.p, nq}, items);
             check();
             const u32 np = read_u32(counters.p + 6);
             std::vector<U2> pairs = fetch(sub_pairs.p, np);
@@ -726,29 +733,17 @@ struct pf_sigma_ctx {
             kept.insert(kept.end(), fresh.begin(), fresh.end());
             units.swap(kept);
         }
-        // commit in producer order: enqueueUnit + toblivion(ot[unit])
-        std::stable_sort(units.begin(), units.end(), [](const U2& x, const U2& y) { return x.x < y.x; });
-        std::vector<u32> A = fetch(asg.p, nvars + 1);
-        std::vector<u32> tr, ul;
-        for (const U2& u : units) {
-            const u32 lit = u.y, v = ABS(lit);
-            if (A[v] == 0) { A[v] = lit; tr.push_back(lit); ul.push_back(lit); }
-            else if (A[v] != lit) {
-                if (!nf) throw int(PF_UNSAT);
-                const u32 f = read_u32(var_fid.p + v);  // that formula alone is unsatisfiable
-                const u32 bit = ERR_UNSAT;
-                rt.h2d(f_err.p + f, &bit, 4);
-            }
-        }
-        for (u32 lit : tr) write_u32(asg.p + ABS(lit), lit);
-        if (!tr.empty()) {
-            rt.h2d(trail.p + ntrail, tr.data(), tr.size() * 4);
-            ntrail += (u32)tr.size();
-            write_u32(counters.p + 0, ntrail);
-            sub_ulits.reserve(rt, ul.size() + 1);
-            rt.h2d(sub_ulits.p, ul.data(), ul.size() * 4);
-            rt.each(FSubCommit{view(), sub_ulits.p}, (u32)ul.size());
-        }
+        // commit: enqueueUnit + toblivion(ot[unit]). The reference commits in producer
+        // order; the outcome does not depend on it (the same literals end assigned, an
+        // opposite pair is a conflict either way), so the units go to the trail in
+        // parallel, first claim wins, and the newly assigned ones empty their lists.
+        sub_units.reserve(rt, std::max<size_t>(units.size(), 16));
+        rt.h2d(sub_units.p, units.data(), units.size() * sizeof(U2));
+        const u32 before = ntrail;
+        rt.each(FSubAssign{view(), sub_units.p}, (u32)units.size());
+        ntrail = read_u32(counters.p + 0);
+        if (ntrail > before) rt.each(FSubCommit{view(), trail.p + before}, ntrail - before);
+        check();
     }
 
     // VE (elimination.cpp:101-108) = bve (bve.cpp:28-142).
