@@ -153,9 +153,8 @@ HD void prop_clause(const PropArgs& a, u32 k) {
 HD void k_prop_lists(const PropArgs& a, u32 k) { prop_lists<false>(a, k); }
 
 #if SIGMA_CUDA
-// Wave A with one warp per pending literal (lanes take the list entries): used
-// when a wave has fewer literals than the launch has warps, where a thread walking
-// a whole list would be the wave's critical path.
+// Wave A with one warp per pending literal (lanes take the list entries), so a
+// long list is never one thread's critical path.
 DEV void prop_lists_warp(const PropArgs& a, u32 k) {
     const Ctx& c = a.c;
     const u32 lane = threadIdx.x & 31u;
@@ -215,11 +214,7 @@ __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
         b.nwork = &w.nwork2[wave & 1];
         if (tid == 0) w.nwork2[(wave + 1) & 1] = 0;
         const u32 nwarps = nth >> 5;
-        if (tail - head < nwarps) {
-            for (u32 i = tid >> 5; i < tail - head; i += nwarps) prop_lists_warp(b, i);
-        } else {
-            for (u32 i = tid; i < tail - head; i += nth) prop_lists<true>(b, i);
-        }
+        for (u32 i = tid >> 5; i < tail - head; i += nwarps) prop_lists_warp(b, i);
         if (!grid_barrier(w.bar, a.c.err)) return;
         const u32 n = vload(b.nwork);
         const u32 nw = n < a.cap_work ? n : a.cap_work;
