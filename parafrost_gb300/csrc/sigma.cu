@@ -128,6 +128,16 @@ struct BatchSplit {
     std::vector<u64> nunit, nres;             // per formula
 };
 
+// Download of a compacted store: clause offsets and learnt flags.
+struct FDownOffsets {
+    const Hdr* hdr; u64* off; uint8_t* learnt;
+    HD void operator()(u32 i) const {
+        const Hdr h = hdr[i];
+        off[i] = h.start;
+        learnt[i] = h_learnt(h.flags) ? 1 : 0;
+    }
+};
+
 // Batch download: formula of every clause (key) with its index (value).
 struct FClauseFid {
     Ctx c; u32* key; u32* val;
@@ -217,6 +227,7 @@ struct pf_sigma_ctx {
     BatchSplit split;
     // host state
     u32 npvs = 0;
+    bool compact = false;          // clause i's literals start at the sum of the earlier sizes
     u32 n_go = 0;                  // elected variables of the formulas that go on (front of pvs)
     u32 perm_off = 0, perm_n = 0;  // range of pv_perm the per-variable stages run over
     bool ot_dirty = false;  // clauses changed since the OT build
@@ -934,7 +945,10 @@ struct pf_sigma_ctx {
 
     // shrinkSimp (simplify.cpp:234-245).
     void gc() {
-        if (!ncls) return;
+        if (!ncls) {
+            compact = true;
+            return;
+        }
         big32a.reserve(rt, (size_t)ncls + 1);
         big32b.reserve(rt, (size_t)ncls + 1);
         big64a.reserve(rt, (size_t)ncls + 1);
@@ -952,6 +966,7 @@ struct pf_sigma_ctx {
         alg_bytes += (4ull * nlits_used + 8ull * ncls) + (4ull * keep_lits + 8ull * keep);
         ncls = keep;
         nlits_used = keep_lits;
+        compact = true;
     }
 
     // resizeCNF (solve.h:684-688).
@@ -1442,6 +1457,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
             return fail("invalid clause (empty, literal out of range or repeated variable)", PF_EINVAL);
         }
         c.uploaded = true;
+        c.compact = false;
         return PF_OK;
     });
 }
@@ -1494,6 +1510,7 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     c.mis_rounds = 0;
     c.rt.launches = 0;
     c.split = BatchSplit();
+    c.compact = false;
     for (int k = 0; k < pf_sigma_ctx::K_COUNT; k++) {
         c.kclock[k].reset();
         c.kbytes[k] = 0;
@@ -1574,7 +1591,18 @@ pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets
     if (ctx->nf) return fail("a formula batch: use pf_sigma_batch_download", PF_ESTATE);
     return guarded([&]() -> pf_status {
         pf_sigma_ctx& c = *ctx;
-        if (lits || offsets || learnt) {
+        if ((lits || offsets || learnt) && c.compact) {
+            // compacted store: the literals are already contiguous in clause order
+            c.big64a.reserve(c.rt, (size_t)c.ncls + 1);
+            DBuf<uint8_t> lrn;
+            lrn.reserve(c.rt, (size_t)c.ncls + 1);
+            if (c.ncls) c.rt.each(FDownOffsets{c.hdr.p, c.big64a.p, lrn.p}, c.ncls);
+            c.write_u64(c.big64a.p + c.ncls, c.nlits_used);
+            if (lits && c.nlits_used) c.rt.d2h(lits, c.lits.p, (size_t)c.nlits_used * 4);
+            if (offsets) c.rt.d2h(offsets, c.big64a.p, ((size_t)c.ncls + 1) * 8);
+            if (learnt && c.ncls) c.rt.d2h(learnt, lrn.p, c.ncls);
+            lrn.free();
+        } else if (lits || offsets || learnt) {
             auto H = c.fetch(c.hdr.p, c.ncls);
             std::vector<u32> L;
             if (lits) L = c.fetch(c.lits.p, c.nlits_used);
