@@ -245,6 +245,19 @@ HD u32 wbcast(u32 v, u32 src) {
 #endif
 }
 
+// Largest f < n with start[f] <= key (start ascending, start[0] <= key): the
+// segment holding item `key` of a list of segments given by their starts.
+template <class T>
+HD u32 upper_segment(const T* start, u32 n, T key) {
+    u32 lo = 0, hi = n;  // answer in [lo, hi)
+    while (hi - lo > 1) {
+        const u32 mid = (lo + hi) >> 1;
+        if (start[mid] <= key) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // Volatile load for values that other threads of the same launch may update.
 HD u32 vload(const u32* p) { return *(const volatile u32*)p; }
 HD u64 vload64(const u64* p) { return *(const volatile u64*)p; }

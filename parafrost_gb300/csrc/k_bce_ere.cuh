@@ -204,6 +204,39 @@ HD void k_ere_pv(const EreArgs& a, u32 k) {
     }
 }
 
+// The same pass with one item per (elected variable, i, j) pair, so a variable
+// with long lists is spread over many threads. perm lists the variables' ranks,
+// cnt/off are per position of perm (pair counts and their exclusive scan).
+HD void k_ere_count(const EreArgs& a, const u32* perm, u64* cnt, u32 q) {
+    const Ctx& c = a.c;
+    const u32 v = a.pvs[perm[q]];
+    const u32 p = V2L(v), n = NEG(p);
+    const u32 sp = c.ot_size[p], sn = c.ot_size[n];
+    cnt[q] = (sp > a.ere_max || sn > a.ere_max) ? 0ull : (u64)sp * sn;
+}
+HD void k_ere_pair(const EreArgs& a, const u32* perm, const u64* off, u32 npos, u32 item) {
+    const Ctx& c = a.c;
+    const u32 q = upper_segment(off, npos, (u64)item);
+    const u32 k = perm[q];
+    const u32 v = a.pvs[k];
+    u32 dx = V2L(v), fx = NEG(dx);
+    if (c.ot_size[dx] > c.ot_size[fx]) swap_t(dx, fx);
+    const ListRef me = list_of(c, dx), other = list_of(c, fx);
+    const u32 r = item - (u32)off[q];
+    const u32 i = r / other.n, j = r - i * other.n;
+    const Hdr hi = c.hdr[me.ids[i]];
+    if (h_deleted(hi.flags)) return;
+    const Hdr hj = c.hdr[other.ids[j]];
+    if (h_deleted(hj.flags)) return;
+    const u32 t = ere_find(c, v, hi, hj, a.ere_clause_max);
+    if (t == NONE) return;
+    const u64 key = ere_key(k, i, j);
+    atom_min64(&a.claim[t], key);
+    const u32 pos = atom_add(a.nrec, 1u);
+    if (pos < a.cap_rec) { a.rec_target[pos] = t; a.rec_key[pos] = key; }
+    else set_err(c, ERR_CAP_SCRATCH);
+}
+
 // Winners delete their target; losers (an earlier resolvent took the same clause)
 // are collected for the ordered fix-up.
 HD void k_ere_resolve(const EreArgs& a, u32 q) {

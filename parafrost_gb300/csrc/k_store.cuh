@@ -26,18 +26,6 @@ struct UploadArgs {
     const u32* f_nv;
 };
 
-// Largest f < n with start[f] <= key (start ascending, start[0] <= key).
-template <class T>
-HD u32 upper_segment(const T* start, u32 n, T key) {
-    u32 lo = 0, hi = n;  // answer in [lo, hi)
-    while (hi - lo > 1) {
-        const u32 mid = (lo + hi) >> 1;
-        if (start[mid] <= key) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
 HD void k_upload_clause(const UploadArgs& a, u32 i) {
     const u64 s = a.off[i] - a.base, e = a.off[i + 1] - a.base;
     u32* l = a.c.lits + s;

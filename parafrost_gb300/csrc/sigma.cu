@@ -71,6 +71,8 @@ struct FBveWrite { BveArgs a; HD void operator()(u32 i) const { k_bve_write(a, i
 struct FBceCount { BceArgs a; HD void operator()(u32 i) const { k_bce_count(a, i); } };
 struct FBceWrite { BceArgs a; HD void operator()(u32 i) const { k_bce_write(a, i); } };
 struct FEre { EreArgs a; HD void operator()(u32 i) const { k_ere_pv(a, i); } };
+struct FEreCount { EreArgs a; const u32* perm; u64* cnt; HD void operator()(u32 q) const { k_ere_count(a, perm, cnt, q); } };
+struct FErePair { EreArgs a; const u32* perm; const u64* off; u32 n; HD void operator()(u32 i) const { k_ere_pair(a, perm, off, n, i); } };
 struct FEreResolve { EreArgs a; HD void operator()(u32 i) const { k_ere_resolve(a, i); } };
 struct FEreFix { EreArgs a; const u64* keys; u32 n; HD void operator()() const { ere_fixup(a, keys, n); } };
 struct FEreSeq { EreArgs a; HD void operator()() const { ere_sequential(a); } };
@@ -906,7 +908,13 @@ struct pf_sigma_ctx {
         a.nlosers = counters.p + 8;
         write_u32(counters.p + 7, 0);
         write_u32(counters.p + 8, 0);
-        pv_each(FEre{a});
+        // one item per (variable, i, j) pair when the pair count fits 32-bit items
+        big64a.reserve(rt, (size_t)perm_n + 1);
+        big64b.reserve(rt, (size_t)perm_n + 1);
+        rt.each(FEreCount{a, pv_perm.p + perm_off, big64a.p}, perm_n);
+        const u64 pairs = scan64(big64a.p, big64b.p, perm_n);
+        if (pairs < 0xFFFFFFF0ull) rt.each(FErePair{a, pv_perm.p + perm_off, big64b.p, perm_n}, (u32)pairs);
+        else pv_each(FEre{a});
         check();
         const u32 nrec = read_u32(counters.p + 7);
         rt.each(FEreResolve{a}, nrec);
