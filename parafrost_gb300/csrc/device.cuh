@@ -110,6 +110,20 @@ HD void warp_sum_add64(u64* p, u64 v) {
 #endif
 }
 
+// Maximum into one word from many threads, one atomic per full warp.
+HD void warp_max_atomic(u32* p, u32 v) {
+#if defined(__CUDA_ARCH__)
+    if (__activemask() != 0xffffffffu) {
+        atomicMax(p, v);
+        return;
+    }
+    v = __reduce_max_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0) atomicMax(p, v);
+#else
+    if (v > *p) *p = v;
+#endif
+}
+
 // Append to a list through one shared counter: the lanes of a warp that append
 // reserve their slots with one atomic. Returns the slot (only meaningful when pred).
 HD u32 warp_append(u32* counter, bool pred) {

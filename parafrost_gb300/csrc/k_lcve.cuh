@@ -45,10 +45,15 @@ struct LcveArgs {
 };
 
 // write_scores (histogram.h:32-41): eligible[v-1] = v, scores[v] = ps*ns (32-bit wrap).
-HD void k_scores(const LcveArgs& a, u32 v) {
-    if (v == 0) return;
-    a.score[v] = a.c.ps[v] * a.c.ns[v];
-    a.order[v - 1] = v;
+// The largest score goes to max_score (it sets how many radix passes the order needs).
+HD void k_scores(const LcveArgs& a, u32* max_score, u32 v) {
+    u32 sc = 0;
+    if (v) {
+        sc = a.c.ps[v] * a.c.ns[v];
+        a.score[v] = sc;
+        a.order[v - 1] = v;
+    }
+    warp_max_atomic(max_score, sc);
 }
 
 HD bool lcve_valid(const Ctx& c, u32 v) {

@@ -41,7 +41,7 @@ struct FGcMove { GcArgs a; HD void operator()(u32 i) const { k_gc_move(a, i); } 
 struct FPropLists { PropArgs a; HD void operator()(u32 i) const { k_prop_lists(a, i); } };
 struct FPropClause { PropArgs a; HD void operator()(u32 i) const { k_prop_clause(a, i); } };
 struct FReduce { Ctx c; HD void operator()(u32 i) const { k_reduce_list(c, i); } };
-struct FScores { LcveArgs a; HD void operator()(u32 i) const { k_scores(a, i); } };
+struct FScores { LcveArgs a; u32* max_score; HD void operator()(u32 i) const { k_scores(a, max_score, i); } };
 struct FRank { LcveArgs a; HD void operator()(u32 i) const { k_rank(a, i); } };
 struct FMisInit { LcveArgs a; MisFront b; HD void operator()(u32 i) const { k_mis_init(a, b, i); } };
 struct FMisCount { LcveArgs a; MisFront f; HD void operator()(u32 i) const { k_mis_count(a, f, i); } };
@@ -85,13 +85,13 @@ struct Perm {
 };
 // Work-order key of elected variable k: descending clause count.
 // Elected variables from n_first on (a batch's stopping formulas) come after the
-// others.
+// others; clause counts above 2^23 share the first place (24-bit keys).
 struct FPvKey {
     Ctx c; const u32* pvs; u32* key; u32* val; u32 n_first;
     HD void operator()(u32 k) const {
         const u32 p = V2L(pvs[k]);
         const u32 occ = c.ot_size[p] + c.ot_size[p + 1];
-        key[k] = (k >= n_first ? 0x80000000u : 0u) | (0x7FFFFFFFu - (occ < 0x7FFFFFFFu ? occ : 0x7FFFFFFFu));
+        key[k] = (k >= n_first ? 0x800000u : 0u) | (0x7FFFFFu - (occ < 0x7FFFFFu ? occ : 0x7FFFFFu));
         val[k] = k;
     }
 };
@@ -509,12 +509,17 @@ struct pf_sigma_ctx {
         a.f_npvs = nf ? f_npvs.p : nullptr;
         const u32 nform = nf ? nf : 1u;
         rt.zero(score.p, (size_t)(nvars + 1) * 4);
-        rt.each(FScores{a}, nvars + 1);
-        // LCV order: stable by score over ascending variables (rSort, sort.h:123-133)
+        write_u32(counters.p + 27, 0);
+        rt.each(FScores{a, counters.p + 27}, nvars + 1);
+        // LCV order: stable by score over ascending variables (rSort, sort.h:123-133);
+        // radix passes only over the bytes the largest score uses
+        const u32 max_score = read_u32(counters.p + 27);
+        int bits = 8;
+        while (bits < 32 && (max_score >> bits)) bits += 8;
         rt.d2d(order_k2.p, score.p + 1, (size_t)nvars * 4);  // keys = score[1..]
-        radix_sort_pairs(order_k2.p, order.p, order_v2.p, rank.p, nvars, 32, radix_hist.p, radix_hscan.p,
+        radix_sort_pairs(order_k2.p, order.p, order_v2.p, rank.p, nvars, bits, radix_hist.p, radix_hscan.p,
                          scan_tmp32.p, rt.stream);
-        rt.launches += 20;
+        rt.launches += 5 * (bits / 8);
         rt.zero(bound.p, (size_t)nform * 8, 0xFF);
         rt.each(FRank{a}, nvars);
         // Independent set by frontier waves. The frontier lists (small / large
@@ -596,9 +601,9 @@ struct pf_sigma_ctx {
         pv_perm.reserve(rt, nvars + 1);
         pv_key.reserve(rt, nvars + 1);
         rt.each(FPvKey{view(), pvs.p, pv_key.p, pv_perm.p, n_go}, npvs);
-        radix_sort_pairs(pv_key.p, pv_perm.p, order_k2.p, order_v2.p, npvs, 32, radix_hist.p, radix_hscan.p,
+        radix_sort_pairs(pv_key.p, pv_perm.p, order_k2.p, order_v2.p, npvs, 24, radix_hist.p, radix_hscan.p,
                          scan_tmp32.p, rt.stream);
-        rt.launches += 20;
+        rt.launches += 15;
     }
 
     // f(k) for every elected variable, in work order, dynamically scheduled.
