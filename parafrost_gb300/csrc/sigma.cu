@@ -12,6 +12,7 @@
 #include "k_sortot.cuh"
 #include "k_store.cuh"
 #include "k_sub.cuh"
+#include "k_sub_warp.cuh"
 #include "prims.cuh"
 #include "runtime.h"
 
@@ -61,6 +62,7 @@ struct FSubSave { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_save(a,
 struct FSubRestore { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_restore(a, i); } };
 struct FSubReach { SubReachArgs a; const u32* off; u32 nq; HD void operator()(u32 i) const { k_sub_reach(a, off, nq, i); } };
 struct FSubReachSize { Ctx c; const U2* units; u32* size; HD void operator()(u32 q) const { k_sub_reach_size(c, units, size, q); } };
+struct FSubWarp { SubArgs a; HD void operator()(u32 k) const { sub_warp_pv(a, k); } };
 struct FSubCommit { Ctx c; const u32* lits; HD void operator()(u32 i) const { k_sub_commit_oblivion(c, lits, i); } };
 struct FSubAssign { Ctx c; const U2* units; HD void operator()(u32 i) const { enqueue_unit(c, units[i].y); } };
 struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) const { k_bve_scratch_need(c, pvs, need, i); } };
@@ -615,6 +617,19 @@ struct pf_sigma_ctx {
     // working set of the elected lists, accumulated by the sort kernel
     u64 pv_bytes() { return read_u64(counters64.p + 1); }
 
+    // One SUB pass over the elected variables (warp per variable).
+    void sub_pass(const SubArgs& a) {
+#if SIGMA_CUDA
+        if (!perm_n) return;
+        ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
+        rt.launches++;
+        sub_warp_k<<<(u32)rt.sms * 8u, 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n, counters.p + 11);
+        ck(cudaGetLastError(), "launch");
+#else
+        pv_each(FSubWarp{a});
+#endif
+    }
+
     // SUB (elimination.cpp:110-129).
     void sub() {
         if (!(opt.sub || opt.ve_plus) || !npvs) return;
@@ -634,7 +649,7 @@ struct pf_sigma_ctx {
         kbytes[K_SUB] += phase_ws;
         if (read_u32(counters.p + 5) == 0) {
             kclock[K_SUB].start(rt);
-            pv_each(FSubPv{a});
+            sub_pass(a);
             kclock[K_SUB].stop(rt);
             check();
             return;
@@ -664,7 +679,7 @@ struct pf_sigma_ctx {
         a.cap_units = (u32)sub_units.n;
         write_u32(counters.p + 4, 0);
         kclock[K_SUB].start(rt);
-        pv_each(FSubPv{a});
+        sub_pass(a);
         kclock[K_SUB].stop(rt);
         check();
         u32 nu = read_u32(counters.p + 4);
@@ -744,7 +759,7 @@ struct pf_sigma_ctx {
             b.pre_lits = sub_pre_lits.p;
             b.run = sub_run.p;
             write_u32(counters.p + 4, 0);
-            pv_each(FSubPv{b});
+            sub_pass(b);
             check();
             const u32 nn = read_u32(counters.p + 4);
             std::vector<U2> fresh = fetch(sub_units.p, nn);
