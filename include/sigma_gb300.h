@@ -173,6 +173,14 @@ pf_status pf_create_ot_noalloc(uint32_t num_vars, const uint32_t* d_lits, const 
 pf_status pf_sigma_upload_batch(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
                                 const uint64_t* clause_begin, const uint32_t* lits, const uint64_t* offsets);
 
+/* Same as pf_sigma_upload_batch with every formula in its own host arrays: formula f
+ * has num_clauses[f] clauses, literals lits[f][offsets[f][c] .. offsets[f][c+1])
+ * (offsets[f][0] need not be 0). Nothing is concatenated on the host: each array is
+ * copied to its place in the store. */
+pf_status pf_sigma_upload_batch_parts(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
+                                      const uint64_t* num_clauses, const uint32_t* const* lits,
+                                      const uint64_t* const* offsets);
+
 /* Same as pf_sigma_upload_batch with lits/offsets in device memory. */
 pf_status pf_sigma_upload_batch_device(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
                                        const uint64_t* clause_begin, const uint32_t* d_lits,

@@ -76,6 +76,7 @@ struct Ctx {
     // one error word per formula (an empty clause ends that formula only)
     const u32* var_fid;
     u32* f_err;
+    uint8_t* res_mark;  // batches: 1 on the last word (the length) of every witness record
 };
 
 constexpr u32 NONE = 0xFFFFFFFFu;

@@ -194,11 +194,13 @@ HD u64 save_clause(const Ctx& c, u64 w, const u32* l, u32 size, u32 witlit) {
     }
     if (pos) { const u32 t = c.resolved[first + pos]; c.resolved[first + pos] = c.resolved[first]; c.resolved[first] = t; }
     c.resolved[w++] = size;
+    if (c.res_mark) c.res_mark[w - 1] = 1;
     return w;
 }
 HD u64 save_witness(const Ctx& c, u64 w, u32 lit) {
     c.resolved[w++] = lit;
     c.resolved[w++] = 1;
+    if (c.res_mark) c.res_mark[w - 1] = 1;
     return w;
 }
 

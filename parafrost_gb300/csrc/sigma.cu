@@ -20,6 +20,7 @@
 #include <array>
 #include <climits>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <set>
 #include <vector>
@@ -123,13 +124,68 @@ struct FPvPartition {
     }
 };
 
-// Host split of a batch's trail and witness stack (kept from the sizes query to
-// the download; cleared by every upload and round).
-struct BatchSplit {
-    bool valid = false;
-    std::vector<u32> trail, resolved;
-    std::vector<std::array<u64, 3>> records;  // witness records: start, length, formula
-    std::vector<u64> nunit, nres;             // per formula
+// Batch upload from separate arrays: offsets moved from each formula's own base
+// to its place in the store.
+struct FRebase {
+    u64* off; const u64* cb; const u64* first; const u64* base; u32 nf;
+    HD void operator()(u32 i) const {
+        const u32 f = upper_segment(cb, nf, (u64)i);
+        off[i] = off[i] - first[f] + base[f];
+    }
+};
+
+// Batch witness split: record starts (the word after a record's length word).
+struct FRecStart {
+    const uint8_t* mark; u32* flag;
+    HD void operator()(u32 i) const { flag[i] = (i == 0 || mark[i - 1]) ? 1u : 0u; }
+};
+struct FRecScatter {
+    const u32* flag; const u32* scan; u32* rstart;
+    HD void operator()(u32 i) const { if (flag[i]) rstart[scan[i]] = i; }
+};
+// Formula (key), index (value) and word count of every record; words per formula.
+struct FRecFid {
+    Ctx c; const u32* rstart; u32 nrec; u32 nwords; u32* key; u32* val; u64* words; u64* f_words;
+    HD void operator()(u32 r) const {
+        const u32 st = rstart[r], en = r + 1 < nrec ? rstart[r + 1] : nwords;
+        const u32 f = c.var_fid[ABS(c.resolved[st])];
+        key[r] = f;
+        val[r] = r;
+        words[r] = en - st;
+        atom_add64(&f_words[f], (u64)(en - st));
+    }
+};
+struct FRecSize {
+    const u64* words; const u32* order; u64* size;
+    HD void operator()(u32 k) const { size[k] = words[order[k]]; }
+};
+// Records in formula order, literals in the formula's numbering, lengths kept.
+struct FRecGather {
+    Ctx c; const u32* rstart; const u32* order; const u32* fid; const u64* words; const u64* off; const u32* f_var;
+    u32* out;
+    HD void operator()(u32 k) const {
+        const u32 r = order[k];
+        const u32 st = rstart[r];
+        const u32 n = (u32)words[r];
+        const u32 shift = 2u * f_var[fid[k]];
+        u32* o = out + off[k];
+        for (u32 j = 0; j + 1 < n; j++) o[j] = c.resolved[st + j] - shift;
+        o[n - 1] = c.resolved[st + n - 1];
+    }
+};
+// Trail split: formula and index of every unit; units per formula.
+struct FUnitFid {
+    Ctx c; u32* key; u32* val; u64* f_units;
+    HD void operator()(u32 i) const {
+        const u32 f = c.var_fid[ABS(c.trail[i])];
+        key[i] = f;
+        val[i] = i;
+        atom_add64(&f_units[f], 1ull);
+    }
+};
+struct FUnitGather {
+    Ctx c; const u32* order; const u32* fid; const u32* f_var; u32* out;
+    HD void operator()(u32 k) const { out[k] = c.trail[order[k]] - 2u * f_var[fid[k]]; }
 };
 
 // Download of a compacted store: clause offsets and learnt flags.
@@ -225,10 +281,10 @@ struct pf_sigma_ctx {
     u32 nf = 0;
     std::vector<u32> h_f_var, h_f_nv;
     DBuf<u32> f_var, var_fid, f_err, f_active, f_npvs, f_group;
+    DBuf<uint8_t> res_mark;  // witness record ends (batches)
     DBuf<u64> f_count;  // [f] live clauses, [nf + f] live literals
     std::vector<int> f_status;
     std::vector<u32> f_phases;
-    BatchSplit split;
     // host state
     u32 npvs = 0;
     bool compact = false;          // clause i's literals start at the sum of the earlier sizes
@@ -277,6 +333,7 @@ struct pf_sigma_ctx {
         c.err = counters.p + 1;
         c.var_fid = nf ? var_fid.p : nullptr;
         c.f_err = nf ? f_err.p : nullptr;
+        c.res_mark = nf ? res_mark.p : nullptr;
         return c;
     }
 
@@ -411,6 +468,10 @@ struct pf_sigma_ctx {
     void ensure_resolved(u64 need) {
         if (need <= resolved.n) return;
         resolved.grow(rt, (size_t)(need + need / 4 + 4096), nresolved);
+        if (nf) {
+            res_mark.grow(rt, resolved.n, nresolved);
+            rt.zero(res_mark.p + nresolved, res_mark.n - nresolved);
+        }
     }
 
     // ------------------------------------------------------------ stages
@@ -1104,6 +1165,82 @@ struct pf_sigma_ctx {
         lrn.free();
     }
 
+    int fid_bits() const {
+        int bits = 8;
+        while (bits < 32 && (nf >> bits)) bits += 8;
+        return bits;
+    }
+
+    // Witness records grouped per formula (records in order inside a formula): the
+    // word count per formula, and with h_out the words in each formula's numbering.
+    void batch_witness(std::vector<u64>& f_words_out, u32* h_out) {
+        const u64 W = nresolved;
+        f_words_out.assign(nf, 0);
+        if (!W) return;
+        if (W >= 0xFFFFFFF0ull) throw std::runtime_error("witness stack too large for 32-bit positions");
+        const u32 w = (u32)W;
+        DBuf<u32> flag, scan, rstart, key, val, k2, v2, out;
+        DBuf<u64> words, size, off, fw;
+        flag.reserve(rt, w);
+        scan.reserve(rt, w);
+        rt.each(FRecStart{res_mark.p, flag.p}, w);
+        const u32 R = scan32(flag.p, scan.p, w);
+        rstart.reserve(rt, R + 1);
+        rt.each(FRecScatter{flag.p, scan.p, rstart.p}, w);
+        key.reserve(rt, R + 1);
+        val.reserve(rt, R + 1);
+        words.reserve(rt, R + 1);
+        fw.reserve(rt, nf);
+        rt.zero(fw.p, (size_t)nf * 8);
+        const Ctx c = view();
+        rt.each(FRecFid{c, rstart.p, R, w, key.p, val.p, words.p, fw.p}, R);
+        rt.d2h(f_words_out.data(), fw.p, (size_t)nf * 8);
+        if (!h_out) return;
+        k2.reserve(rt, R + 1);
+        v2.reserve(rt, R + 1);
+        radix_hist.reserve(rt, radix_hist_elems(R));
+        radix_hscan.reserve(rt, radix_hist_elems(R));
+        scan_tmp32.reserve(rt, scan_tmp_elems(radix_hist_elems(R)) + 4);
+        const int bits = fid_bits();
+        radix_sort_pairs(key.p, val.p, k2.p, v2.p, R, bits, radix_hist.p, radix_hscan.p, scan_tmp32.p, rt.stream);
+        rt.launches += 5 * (bits / 8);
+        size.reserve(rt, R + 1);
+        off.reserve(rt, R + 1);
+        rt.each(FRecSize{words.p, val.p, size.p}, R);
+        scan64(size.p, off.p, R);
+        out.reserve(rt, w);
+        rt.each(FRecGather{c, rstart.p, val.p, key.p, words.p, off.p, f_var.p, out.p}, R);
+        rt.d2h(h_out, out.p, (size_t)w * 4);
+    }
+
+    // Trail units grouped per formula, in the formula's numbering.
+    void batch_units(std::vector<u64>& f_units_out, u32* h_out) {
+        f_units_out.assign(nf, 0);
+        const u32 n = ntrail;
+        if (!n) return;
+        DBuf<u32> key, val, k2, v2, out;
+        DBuf<u64> fu;
+        key.reserve(rt, n);
+        val.reserve(rt, n);
+        fu.reserve(rt, nf);
+        rt.zero(fu.p, (size_t)nf * 8);
+        const Ctx c = view();
+        rt.each(FUnitFid{c, key.p, val.p, fu.p}, n);
+        rt.d2h(f_units_out.data(), fu.p, (size_t)nf * 8);
+        if (!h_out) return;
+        k2.reserve(rt, n);
+        v2.reserve(rt, n);
+        radix_hist.reserve(rt, radix_hist_elems(n));
+        radix_hscan.reserve(rt, radix_hist_elems(n));
+        scan_tmp32.reserve(rt, scan_tmp_elems(radix_hist_elems(n)) + 4);
+        const int bits = fid_bits();
+        radix_sort_pairs(key.p, val.p, k2.p, v2.p, n, bits, radix_hist.p, radix_hscan.p, scan_tmp32.p, rt.stream);
+        rt.launches += 5 * (bits / 8);
+        out.reserve(rt, n);
+        rt.each(FUnitGather{c, val.p, key.p, f_var.p, out.p}, n);
+        rt.d2h(h_out, out.p, (size_t)n * 4);
+    }
+
     // Formula of a literal of the store, on the host.
     u32 host_fid(u32 lit) const {
         const u32 v = ABS(lit);
@@ -1354,6 +1491,9 @@ struct BatchSpec {
     u32 nf;
     const uint32_t* num_vars;
     const uint64_t* clause_begin;
+    // formulas in separate host arrays (null: one concatenated lits/offsets pair)
+    const uint32_t* const* part_lits = nullptr;
+    const uint64_t* const* part_offsets = nullptr;
 };
 
 static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint32_t* lits, const uint64_t* offsets,
@@ -1367,7 +1507,15 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         pf_sigma_ctx& c = *ctx;
         Runtime& rt = c.rt;
         u64 off0 = 0, offn = 0;
-        if (device) {
+        const bool parts = batch && batch->part_lits;
+        if (parts) {
+            for (u32 f = 0; f < batch->nf; f++) {
+                const u64 nc = batch->clause_begin[f + 1] - batch->clause_begin[f];
+                const u64* o = batch->part_offsets[f];
+                if (o[nc] < o[0]) return fail("offsets not ascending", PF_EINVAL);
+                offn += o[nc] - o[0];
+            }
+        } else if (device) {
             rt.d2h(&off0, offsets, 8);
             rt.d2h(&offn, offsets + num_clauses, 8);
         } else {
@@ -1380,8 +1528,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         c.nvars = num_vars;
         c.D = 2 * (num_vars + 1);
         c.nf = batch ? batch->nf : 0u;
-        c.split = BatchSplit();
-        c.fc_cls.clear();
+            c.fc_cls.clear();
         c.fc_lits.clear();
         c.ncls = (u32)num_clauses;
         c.nlits_used = L;
@@ -1428,7 +1575,34 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         DBuf<uint8_t> dlearnt;
         const u64* off_ptr = offsets;
         const uint8_t* learnt_ptr = learnt;
-        if (device) {
+        if (parts) {
+            // each formula's literals and offsets straight to their place; offsets
+            // are rebased on the device
+            doff.reserve(rt, num_clauses + 1);
+            std::vector<u64> first(batch->nf), base(batch->nf);
+            u64 at = 0;
+            for (u32 f = 0; f < batch->nf; f++) {
+                const u64 cb = batch->clause_begin[f], nc = batch->clause_begin[f + 1] - cb;
+                const u64* o = batch->part_offsets[f];
+                const u64 len = o[nc] - o[0];
+                first[f] = o[0];
+                base[f] = at;
+                if (len) rt.h2d(c.lits.p + at, batch->part_lits[f] + o[0], len * 4);
+                if (nc) rt.h2d(doff.p + cb, o, nc * 8);
+                at += len;
+            }
+            c.write_u64(doff.p + num_clauses, at);
+            DBuf<u64> dfirst, dbase, dcb;
+            dfirst.reserve(rt, batch->nf);
+            dbase.reserve(rt, batch->nf);
+            dcb.reserve(rt, batch->nf + 1);
+            rt.h2d(dfirst.p, first.data(), batch->nf * 8);
+            rt.h2d(dbase.p, base.data(), batch->nf * 8);
+            rt.h2d(dcb.p, batch->clause_begin, (batch->nf + 1) * 8);
+            if (num_clauses) rt.each(FRebase{doff.p, dcb.p, dfirst.p, dbase.p, batch->nf}, (u32)num_clauses);
+            rt.sync();
+            off_ptr = doff.p;
+        } else if (device) {
             rt.d2d(c.lits.p, lits + off0, L * 4);
         } else {
             doff.reserve(rt, num_clauses + 1);
@@ -1471,6 +1645,8 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
             c.bound.reserve(rt, 2 * (size_t)nf + 2);
             c.f_status.assign(nf, PF_OK);
             c.f_phases.assign(nf, 0);
+            c.res_mark.reserve(rt, c.resolved.n);
+            rt.zero(c.res_mark.p, c.res_mark.n);
             a = UploadArgs{c.view(), off_ptr, learnt_ptr, off0, nf, dcls.p, c.f_var.p, dnv.p};
         }
         rt.each(FUpload{a}, (u32)num_clauses);
@@ -1522,6 +1698,26 @@ pf_status pf_sigma_upload_batch(pf_sigma_ctx* ctx, uint32_t num_formulas, const 
     return upload_batch(ctx, num_formulas, num_vars, clause_begin, lits, offsets, false);
 }
 
+pf_status pf_sigma_upload_batch_parts(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
+                                      const uint64_t* num_clauses, const uint32_t* const* lits,
+                                      const uint64_t* const* offsets) {
+    if (!ctx) return fail("null context", PF_EINVAL);
+    if (!num_formulas || !num_vars || !num_clauses || !lits || !offsets) return fail("empty batch", PF_EINVAL);
+    std::vector<uint64_t> cb(num_formulas + 1, 0);
+    u64 total_vars = 0;
+    for (u32 f = 0; f < num_formulas; f++) {
+        if (!lits[f] || !offsets[f]) return fail("null formula", PF_EINVAL);
+        if (num_vars[f] >= (1u << 30)) return fail("too many variables", PF_EINVAL);
+        cb[f + 1] = cb[f] + num_clauses[f];
+        total_vars += (num_vars[f] + 15u) & ~15u;
+    }
+    if (total_vars == 0) return fail("batch without variables", PF_EINVAL);
+    if (total_vars >= (1u << 30)) return fail("too many variables", PF_EINVAL);
+    BatchSpec b{num_formulas, num_vars, cb.data(), lits, offsets};
+    // lits/offsets of the concatenated form are unused with parts; pass non-null markers
+    return upload_common(ctx, (u32)total_vars, lits[0], offsets[0], cb[num_formulas], nullptr, false, &b);
+}
+
 pf_status pf_sigma_upload_batch_device(pf_sigma_ctx* ctx, uint32_t num_formulas, const uint32_t* num_vars,
                                        const uint64_t* clause_begin, const uint32_t* d_lits,
                                        const uint64_t* d_offsets) {
@@ -1537,7 +1733,6 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     c.alg_bytes = 0;
     c.mis_rounds = 0;
     c.rt.launches = 0;
-    c.split = BatchSplit();
     c.compact = false;
     for (int k = 0; k < pf_sigma_ctx::K_COUNT; k++) {
         c.kclock[k].reset();
@@ -1654,28 +1849,6 @@ pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets
 // Clauses are grouped per formula on the device (a stable sort of the store by
 // formula); the trail and the witness stack are split on the host, with literals
 // back in each formula's own numbering.
-static void batch_split(pf_sigma_ctx& c, BatchSplit& b) {
-    const u32 nf = c.nf;
-    if (b.valid) return;
-    b.trail = c.fetch(c.trail.p, c.ntrail);
-    b.resolved = c.fetch(c.resolved.p, c.nresolved);
-    b.nunit.assign(nf, 0);
-    b.nres.assign(nf, 0);
-    for (u32 lit : b.trail) b.nunit[c.host_fid(lit)]++;
-    b.records.clear();
-    for (u64 pos = b.resolved.size(); pos > 0;) {
-        const u64 len = b.resolved[pos - 1];
-        if (len == 0 || len + 1 > pos) throw std::runtime_error("malformed witness stack");
-        const u64 start = pos - 1 - len;
-        const u32 f = c.host_fid(b.resolved[start]);
-        b.records.push_back({start, len, f});
-        b.nres[f] += len + 1;
-        pos = start;
-    }
-    std::reverse(b.records.begin(), b.records.end());
-    b.valid = true;
-}
-
 pf_status pf_sigma_batch_result_sizes(pf_sigma_ctx* ctx, int32_t* status, uint32_t* phases, uint64_t* num_clauses,
                                       uint64_t* num_literals, uint64_t* num_units, uint64_t* num_resolved) {
     if (!ctx || !ctx->uploaded) return fail("no formula", PF_ESTATE);
@@ -1683,15 +1856,16 @@ pf_status pf_sigma_batch_result_sizes(pf_sigma_ctx* ctx, int32_t* status, uint32
     return guarded([&]() -> pf_status {
         pf_sigma_ctx& c = *ctx;
         if (c.fc_cls.size() != c.nf) c.count_formulas();
-        BatchSplit& b = c.split;
-        if (num_units || num_resolved) batch_split(c, b);
+        std::vector<u64> nunit, nres;
+        if (num_units) c.batch_units(nunit, nullptr);
+        if (num_resolved) c.batch_witness(nres, nullptr);
         for (u32 f = 0; f < c.nf; f++) {
             if (status) status[f] = c.f_status[f];
             if (phases) phases[f] = c.f_phases[f];
             if (num_clauses) num_clauses[f] = c.fc_cls[f];
             if (num_literals) num_literals[f] = c.fc_lits[f];
-            if (num_units) num_units[f] = b.nunit[f];
-            if (num_resolved) num_resolved[f] = b.nres[f];
+            if (num_units) num_units[f] = nunit[f];
+            if (num_resolved) num_resolved[f] = nres[f];
         }
         return PF_OK;
     });
@@ -1705,28 +1879,9 @@ pf_status pf_sigma_batch_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* o
         pf_sigma_ctx& c = *ctx;
         const u32 nf = c.nf;
         if (lits || offsets || learnt) c.batch_clauses_to(lits, offsets, learnt);
-        auto local = [&](u32 lit, u32 f) { return lit - 2u * c.h_f_var[f]; };
-        if (units || resolved) {
-            BatchSplit& b = c.split;
-            batch_split(c, b);
-            if (units) {
-                std::vector<u64> ubeg(nf + 1, 0);
-                for (u32 f = 0; f < nf; f++) ubeg[f + 1] = ubeg[f] + b.nunit[f];
-                for (u32 lit : b.trail) {
-                    const u32 f = c.host_fid(lit);
-                    units[ubeg[f]++] = local(lit, f);
-                }
-            }
-            if (resolved) {
-                std::vector<u64> rbeg(nf + 1, 0);
-                for (u32 f = 0; f < nf; f++) rbeg[f + 1] = rbeg[f] + b.nres[f];
-                for (const auto& r : b.records) {
-                    u64& w = rbeg[r[2]];
-                    for (u64 j = 0; j < r[1]; j++) resolved[w++] = local(b.resolved[r[0] + j], (u32)r[2]);
-                    resolved[w++] = (u32)r[1];
-                }
-            }
-        }
+        std::vector<u64> counts;
+        if (units) c.batch_units(counts, units);
+        if (resolved) c.batch_witness(counts, resolved);
         if (eliminated) {
             const std::vector<uint8_t> vs = c.fetch(c.vstate.p, c.nvars + 1);
             u64 w = 0;
@@ -1882,6 +2037,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     for (auto* b : b64) b->free();
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
     c.mis_word.free();
+    c.res_mark.free();
     c.mis_big_a.free();
     c.mis_big_b.free();
     c.pv_perm.free();

@@ -24,7 +24,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .options import Options
-from .sigma import Result, Simplifier, pack_batch, lits_offsets_begin
+from .sigma import Result, Simplifier
 
 
 def estimate_footprint(num_vars: int, num_clauses: int, num_literals: int) -> int:
@@ -177,9 +177,7 @@ class Server:
     def _serve_batch(self, ctx: Simplifier, batch: list, bi: int) -> None:
         forms = [r.formula for r in batch]
         try:
-            nv, lits, off = pack_batch(forms)
-            cb, lits, off = lits_offsets_begin(forms, lits, off)
-            ctx.upload_batch(nv, cb, lits, off)
+            ctx.awaken_batch(forms)
             st = ctx.sigmify()
             self._launches += st.kernel_launches
             out = ctx.batch_results()

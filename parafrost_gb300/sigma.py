@@ -80,6 +80,8 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     lib.pf_sigma_write_dump.restype = ctypes.c_int
     lib.pf_sigma_upload_batch.argtypes = [_VP, _U32, _VP, _VP, _VP, _VP]
     lib.pf_sigma_upload_batch.restype = ctypes.c_int
+    lib.pf_sigma_upload_batch_parts.argtypes = [_VP, _U32, _VP, _VP, _VP, _VP]
+    lib.pf_sigma_upload_batch_parts.restype = ctypes.c_int
     lib.pf_sigma_upload_batch_device.argtypes = [_VP, _U32, _VP, _VP, _VP, _VP]
     lib.pf_sigma_upload_batch_device.restype = ctypes.c_int
     lib.pf_sigma_batch_result_sizes.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
@@ -224,9 +226,19 @@ class Simplifier:
     # ---- formula batches
     def awaken_batch(self, formulas) -> None:
         """Upload a batch: formulas is a sequence of (num_vars, lits, offsets) in each
-        formula's own numbering."""
-        nv, lits, offs = pack_batch(formulas)
-        self.upload_batch(nv, *lits_offsets_begin(formulas, lits, offs))
+        formula's own numbering (each formula copied from its own arrays)."""
+        nf = len(formulas)
+        arrs = [(np.ascontiguousarray(l, dtype=np.uint32), np.ascontiguousarray(o, dtype=np.uint64))
+                for _, l, o in formulas]
+        nv = np.array([f[0] for f in formulas], dtype=np.uint32)
+        nc = np.array([o.size - 1 for _, o in arrs], dtype=np.uint64)
+        dummy = np.zeros(1, np.uint32)  # stands for an empty formula's literal array
+        lp = (ctypes.c_void_p * nf)(*[l.ctypes.data if l.size else dummy.ctypes.data for l, _ in arrs])
+        op = (ctypes.c_void_p * nf)(*[o.ctypes.data for _, o in arrs])
+        self._keep = (arrs, dummy)  # the arrays must live through the call
+        self._check(self.lib.pf_sigma_upload_batch_parts(self.h, nf, _ptr(nv), _ptr(nc), lp, op))
+        self._keep = None
+        self.batch_vars = nv.copy()
 
     def upload_batch(self, num_vars: np.ndarray, clause_begin: np.ndarray, lits: np.ndarray,
                      offsets: np.ndarray) -> None:
