@@ -80,7 +80,7 @@ HD void k_rank(const LcveArgs& a, u32 p) {
 // Each wave processes only the vertices decided in the previous one. A neighbour
 // shared through several clauses is counted and decremented once per clause.
 // Vertices with more than MIS_WARP_MIN_OCC clauses are handled by a whole warp.
-constexpr u32 MIS_WARP_MIN_OCC = 12;
+constexpr u32 MIS_WARP_MIN_OCC = 32;
 
 struct MisFront {
     u32* small;   // next frontier, small adjacency
