@@ -110,15 +110,17 @@ HD void warp_sum_add64(u64* p, u64 v) {
 #endif
 }
 
-// Maximum into one word from many threads, one atomic per full warp.
+// Maximum into one word from many threads: one atomic per full warp, and only
+// when the warp's value exceeds what the word already holds (the word settles
+// early, so most warps only read it).
 HD void warp_max_atomic(u32* p, u32 v) {
 #if defined(__CUDA_ARCH__)
     if (__activemask() != 0xffffffffu) {
-        atomicMax(p, v);
+        if (v > *(volatile u32*)p) atomicMax(p, v);
         return;
     }
     v = __reduce_max_sync(0xffffffffu, v);
-    if ((threadIdx.x & 31) == 0) atomicMax(p, v);
+    if ((threadIdx.x & 31) == 0 && v > *(volatile u32*)p) atomicMax(p, v);
 #else
     if (v > *p) *p = v;
 #endif

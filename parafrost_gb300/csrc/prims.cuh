@@ -119,6 +119,116 @@ void excl_scan(const Tin* in, T* out, size_t n, T* total, T* tmp, cudaStream_t s
     scan_down_k<Tin, T><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, tmp);
 }
 
+// Single-pass exclusive scan (decoupled look-back): each tile takes its index from
+// a counter in launch order, publishes its aggregate, adds the aggregates (or the
+// first inclusive prefix) of the tiles before it, publishes its inclusive prefix
+// and scans itself. Flags carry the scan's epoch, so nothing is cleared between
+// scans; a tile index counter keeps running and base is where this scan's tiles
+// start. A look-back wait that runs out records ERR_ITER in err.
+struct Scan1State {
+    u64* agg;       // per tile
+    u64* incl;      // per tile
+    u32* flag;      // per tile: epoch << 2 | 1 (aggregate) or | 2 (inclusive)
+    u32* counter;   // tile index counter
+    u32* err;
+};
+
+template <class Tin, class T>
+__global__ void __launch_bounds__(kScanThreads) scan1_k(const Tin* in, T* out, size_t n, T* total, Scan1State st,
+                                                       u32 base, u32 epoch) {
+    __shared__ u32 tile_s;
+    __shared__ T ws[kScanThreads / 32];
+    __shared__ T carry_s;
+    if (threadIdx.x == 0) tile_s = atomicAdd(st.counter, 1u) - base;
+    __syncthreads();
+    const u32 tile = tile_s;
+    const size_t nb = (n + kScanTile - 1) / kScanTile;
+    const size_t t0 = (size_t)tile * kScanTile;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // tile aggregate
+    T s = 0;
+    for (int k = 0; k < kScanItems; k++) {
+        const size_t i = t0 + (size_t)k * kScanThreads + threadIdx.x;
+        if (i < n) s += (T)in[i];
+    }
+    for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) ws[warp] = s;
+    __syncthreads();
+    if (warp == 0) {
+        // warp 0 publishes the aggregate and looks back 32 tiles at a time: it waits
+        // for their flags, adds the aggregates after the nearest inclusive prefix and
+        // stops there (or moves 32 tiles further back)
+        T a = 0;
+        for (int w = 0; w < kScanThreads / 32; w++) a += ws[w];
+        T prefix = 0;
+        if (lane == 0) {
+            if (tile == 0) st.incl[0] = (u64)a;
+            else st.agg[tile] = (u64)a;
+            __threadfence();
+            atomicExch(&st.flag[tile], (epoch << 2) | (tile == 0 ? 2u : 1u));
+        }
+        __syncwarp();
+        bool late = false;
+        for (long long top = (long long)tile - 1; top >= 0 && !late; top -= 32) {
+            const long long p = top - lane;
+            u32 f = (epoch << 2) | 1u;  // lanes past tile 0 add nothing
+            u32 it = 0;
+            if (p >= 0) {
+                while (((f = *(volatile u32*)&st.flag[p]) >> 2) != epoch) {
+                    if (++it > (1u << 24)) {
+                        late = true;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            late = __any_sync(0xffffffffu, late);
+            if (late) break;
+            __threadfence();
+            // lanes 0.. look at tiles top, top-1, ...: the first inclusive one stops the walk
+            const u32 incl_mask = __ballot_sync(0xffffffffu, p >= 0 && (f & 3u) == 2u);
+            const int stop = incl_mask ? __ffs(incl_mask) - 1 : 32;
+            T v = 0;
+            if (p >= 0 && lane <= stop) {
+                v = lane == stop ? (T)(*(volatile u64*)&st.incl[p]) : (T)(*(volatile u64*)&st.agg[p]);
+            }
+            for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            prefix += __shfl_sync(0xffffffffu, v, 0);
+            if (incl_mask) break;
+        }
+        if (lane == 0) {
+            if (late) atomicOr(st.err, ERR_ITER);
+            if (tile != 0) {
+                st.incl[tile] = (u64)(prefix + a);
+                __threadfence();
+                atomicExch(&st.flag[tile], (epoch << 2) | 2u);
+            }
+            if (tile + 1 == nb && total) *total = prefix + a;
+            carry_s = prefix;
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < kScanItems; k++) {
+        const size_t i = t0 + (size_t)k * kScanThreads + threadIdx.x;
+        const T v = i < n ? (T)in[i] : T(0);
+        const T incl = warp_incl_scan(v);
+        if (lane == 31) ws[warp] = incl;
+        __syncthreads();
+        T wpre = 0, btot = 0;
+        for (int w = 0; w < kScanThreads / 32; w++) {
+            if (w < warp) wpre += ws[w];
+            btot += ws[w];
+        }
+        const T carry = carry_s;
+        if (i < n) out[i] = carry + wpre + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry_s = carry + btot;
+        __syncthreads();
+    }
+}
+
+inline size_t scan1_tiles(size_t n) { return (n + kScanTile - 1) / kScanTile; }
+
 // ---------------------------------------------------------------- radix sort
 constexpr int kRadixThreads = 256;
 constexpr int kRadixChunks = 16;  // items per thread per tile

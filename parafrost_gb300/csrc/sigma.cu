@@ -371,6 +371,48 @@ struct pf_sigma_ctx {
     void write_u64(u64* d, u64 v) { rt.h2d(d, &v, 8); }
 
     // exclusive scans
+#if SIGMA_CUDA
+    // single-pass scans: tile state kept across scans (flags tagged with an epoch)
+    DBuf<u64> scan1_agg, scan1_incl, scan1_total;
+    DBuf<u32> scan1_flag, scan1_ctl;
+    u32 scan1_epoch = 0, scan1_base = 0;
+    template <class Tin, class T>
+    T scan1(const Tin* in, T* out, size_t n) {
+        const size_t tiles = scan1_tiles(n);
+        if (!scan1_ctl.p || scan1_base > 0x7FFFFFFFu || scan1_epoch >= 0x3FFFFFFFu) {
+            scan1_ctl.reserve(rt, 4);
+            rt.zero(scan1_ctl.p, 16);
+            scan1_base = 0;
+            if (scan1_flag.p) rt.zero(scan1_flag.p, scan1_flag.bytes());
+            scan1_epoch = 0;
+        }
+        if (tiles > scan1_flag.n) {
+            const size_t cap = tiles + tiles / 2 + 64;
+            scan1_agg.reserve(rt, cap);
+            scan1_incl.reserve(rt, cap);
+            scan1_flag.reserve(rt, cap);
+            rt.zero(scan1_flag.p, scan1_flag.bytes());
+        }
+        scan1_total.reserve(rt, 2);
+        T* total = (T*)scan1_total.p;
+        if (n == 0) {
+            rt.zero(total, sizeof(T));
+        } else {
+            Scan1State st{scan1_agg.p, scan1_incl.p, scan1_flag.p, scan1_ctl.p, counters.p + 1};
+            rt.launches++;
+            scan1_k<Tin, T><<<(unsigned)tiles, kScanThreads, 0, rt.stream>>>(in, out, n, total, st, scan1_base,
+                                                                             ++scan1_epoch);
+            ck(cudaGetLastError(), "launch");
+            scan1_base += (u32)tiles;
+        }
+        T h = 0;
+        rt.d2h(&h, total, sizeof(T));
+        return h;
+    }
+    u32 scan32(const u32* in, u32* out, size_t n) { return scan1<u32, u32>(in, out, n); }
+    template <class Tin>
+    u64 scan64(const Tin* in, u64* out, size_t n) { return scan1<Tin, u64>(in, out, n); }
+#else
     u32 scan32(const u32* in, u32* out, size_t n) {
         scan_tmp32.reserve(rt, scan_tmp_elems(n) + 2);
         u32* total = scan_tmp32.p + scan_tmp32.n - 1;
@@ -386,6 +428,7 @@ struct pf_sigma_ctx {
         rt.launches += 3;
         return read_u64(total);
     }
+#endif
 
     // ------------------------------------------------------------ dumps
     void rec(u32 kind, u32 ph, u32 stage, const std::vector<u32>& d) {
@@ -2038,6 +2081,13 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
     c.mis_word.free();
     c.res_mark.free();
+#if SIGMA_CUDA
+    c.scan1_agg.free();
+    c.scan1_incl.free();
+    c.scan1_total.free();
+    c.scan1_flag.free();
+    c.scan1_ctl.free();
+#endif
     c.mis_big_a.free();
     c.mis_big_b.free();
     c.pv_perm.free();
