@@ -13,7 +13,7 @@
 // Units go straight to the trail through a compare-and-swap on their variable.
 //
 // Elected variables share no clause, so molten flags and in-place edits stay
-// private. The decision lives in k_bve_analyze.cuh.
+// private. The decision lives in k_bve_warp.cuh (warp form) and k_bve_analyze.cuh.
 #pragma once
 
 #include "cnf.cuh"
@@ -78,56 +78,6 @@ HD bool merge_into(u32 x, const u32* a, u32 n1, const u32* b, u32 n2, u32* out, 
     while (i < n1) { const u32 l = a[i++]; if (ABS(l) != x) out[on++] = l; }
     while (j < n2) { const u32 l = b[j++]; if (ABS(l) != x) out[on++] = l; }
     return true;
-}
-
-// Step 1 for one elected variable: the decision on a shared-memory copy of its lists
-// when they fit the slot, else on global memory.
-HD void bve_analyze_one(const BveArgs& a, u32 k, u32* slot) {
-    VeOpts o;
-    o.ve_clause_max = a.ve_clause_max;
-    o.ve_lbound = a.ve_lbound;
-    o.xor_max_arity = a.xor_max_arity;
-    VeResult r;
-    SmemPv s;
-    if (slot && s.stage(a.c, a.pvs[k], slot)) {
-        r = pv_bve_decide(s, o);
-    } else {
-        GlobalPv g;
-        g.init(a.c, a.pvs[k], a.scr + a.scr_off[k]);
-        r = pv_bve_decide(g, o);
-    }
-    a.type[k] = r.type;
-    a.porgs[k] = r.porgs;
-    a.norgs[k] = r.norgs;
-    a.def[k] = r.def;
-    a.ncls[k] = r.ncls;
-    a.nlits[k] = r.nlits;
-    a.nwit[k] = r.nwit;
-}
-
-#if SIGMA_CUDA
-// One thread per elected variable, PV_SLOT words of shared memory per thread, warps
-// taking 32 variables at a time in work order (perm) from a shared counter.
-constexpr int kBveThreads = 128;
-__global__ void __launch_bounds__(kBveThreads) bve_analyze_k(BveArgs a, const u32* perm, u32* next) {
-    extern __shared__ u32 smem[];
-    u32* slot = smem + threadIdx.x * PV_SLOT;
-    const u32 lane = threadIdx.x & 31u;
-    while (true) {
-        u32 base = 0;
-        if (lane == 0) base = atomicAdd(next, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= a.npvs) break;
-        if (base + lane < a.npvs) bve_analyze_one(a, perm[base + lane], slot);
-        __syncwarp();
-    }
-}
-#endif
-
-// Emulation entry of the staged path: the slot is a local array.
-HD void k_bve_analyze(const BveArgs& a, u32 k) {
-    u32 slot[PV_SLOT];
-    bve_analyze_one(a, k, slot);
 }
 
 // Step 1 with one warp per elected variable (k_bve_warp.cuh); variables too large

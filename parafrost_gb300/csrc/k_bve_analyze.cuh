@@ -1,13 +1,10 @@
 // BVE step 1 (the decision of ParaFROST::bve, src/cpu/bve.cpp:37-142) over a view
 // of one elected variable's two occurrence lists.
 //
-// The decision is a long sequence of dependent reads (gate finders, resolvent
-// counts) over a handful of clauses. Reading them straight from HBM makes every
-// thread one chain of cache misses, so each thread first copies its variable's
-// lists (ids, headers, literals) into its own shared-memory slot with independent
-// loads (SmemPv), and the decision then runs on that copy; molten flags are written
-// through to the clause store, where the write step reads them. Variables whose
-// lists do not fit the slot run the same code on global memory (GlobalPv).
+// This is the per-thread form of the decision, reading the lists straight from the
+// clause store (GlobalPv). The kernel runs the warp form (k_bve_warp.cuh); a
+// variable whose lists do not fit the warp's shared-memory slot runs this one on
+// lane 0.
 //
 // View entries are numbered 0..np-1 (the positive list ot[2v]) and np..np+nn-1 (the
 // negative list ot[2v+1]); side s of literal l is l & 1.
@@ -46,71 +43,6 @@ struct GlobalPv {
     HD const u32* lits(u32 i) const { return c->lits + c->hdr[id(i)].start; }
     HD void set_molten(u32 i, bool m) const { sigma::set_molten(*c, id(i), m); }
     HD u32* scratch() const { return scr; }
-};
-
-// Per-thread shared-memory slot: [np, nn, id[KC], size[KC], sig[KC], flags[KC],
-// start[KC], lits[KL]], padded to an odd word count so that the 32 slots of a warp
-// fall in 32 different banks.
-constexpr u32 PV_KC = 16;
-constexpr u32 PV_KL = 64;
-constexpr u32 PV_SLOT = ((2 + 5 * PV_KC + PV_KL) | 1u);
-
-struct SmemPv {
-    const Ctx* c;
-    u32 v, np, nn;
-    u32* S;
-    u32 scr[PV_KC + 2];
-
-    enum : u32 { O_ID = 2, O_SIZE = 2 + PV_KC, O_SIG = 2 + 2 * PV_KC, O_FLAGS = 2 + 3 * PV_KC,
-                 O_START = 2 + 4 * PV_KC, O_LITS = 2 + 5 * PV_KC };
-
-    // Copies the lists into the slot; false when they do not fit.
-    HD bool stage(const Ctx& cc, u32 var, u32* slot) {
-        c = &cc;
-        v = var;
-        S = slot;
-        const u32 p = V2L(var);
-        np = cc.ot_size[p];
-        nn = cc.ot_size[p + 1];
-        if (np + nn > PV_KC) return false;
-        const u32* lp = cc.ot_refs + cc.ot_off[p];
-        const u32* ln = cc.ot_refs + cc.ot_off[p + 1];
-        for (u32 i = 0; i < np; i++) S[O_ID + i] = lp[i];
-        for (u32 i = 0; i < nn; i++) S[O_ID + np + i] = ln[i];
-        u32 total = 0;
-        for (u32 i = 0; i < np + nn; i++) {
-            const Hdr h = cc.hdr[S[O_ID + i]];
-            S[O_SIZE + i] = h.size;
-            S[O_SIG + i] = h.sig;
-            S[O_FLAGS + i] = h.flags;
-            S[O_START + i] = total;
-            total += h.size;
-            // keep the global start to copy the literals
-            scr[i < PV_KC + 2 ? i : 0] = h.start;
-        }
-        if (total > PV_KL) return false;
-        for (u32 i = 0; i < np + nn; i++) {
-            const u32* src = cc.lits + scr[i];
-            u32* dst = S + O_LITS + S[O_START + i];
-            const u32 sz = S[O_SIZE + i];
-            for (u32 k = 0; k < sz; k++) dst[k] = src[k];
-        }
-        return true;
-    }
-    HD u32 n(u32 side) const { return side ? nn : np; }
-    HD u32 base(u32 side) const { return side ? np : 0u; }
-    HD u32 id(u32 i) const { return S[O_ID + i]; }
-    HD u32 size(u32 i) const { return S[O_SIZE + i]; }
-    HD u32 sig(u32 i) const { return S[O_SIG + i]; }
-    HD u32 flags(u32 i) const { return S[O_FLAGS + i]; }
-    HD const u32* lits(u32 i) const { return S + O_LITS + S[O_START + i]; }
-    HD void set_molten(u32 i, bool m) {
-        const u32 f = S[O_FLAGS + i];
-        const u32 nf = m ? (f | F_MOLTEN) : (f & ~F_MOLTEN);
-        S[O_FLAGS + i] = nf;
-        c->hdr[S[O_ID + i]].flags = nf;
-    }
-    HD u32* scratch() { return scr; }
 };
 
 // ---------------------------------------------------------------- helpers

@@ -67,8 +67,6 @@ struct FSubWarp { SubArgs a; HD void operator()(u32 k) const { sub_warp_pv(a, k)
 struct FSubCommit { Ctx c; const u32* lits; HD void operator()(u32 i) const { k_sub_commit_oblivion(c, lits, i); } };
 struct FSubAssign { Ctx c; const U2* units; HD void operator()(u32 i) const { enqueue_unit(c, units[i].y); } };
 struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) const { k_bve_scratch_need(c, pvs, need, i); } };
-struct FBveAnalyze { BveArgs a; HD void operator()(u32 i) const { bve_analyze_one(a, i, nullptr); } };
-struct FBveAnalyzeStaged { BveArgs a; HD void operator()(u32 i) const { k_bve_analyze(a, i); } };
 struct FBveWarp { BveArgs a; HD void operator()(u32 i) const { k_bve_warp(a, i); } };
 struct FBveWrite { BveArgs a; HD void operator()(u32 i) const { k_bve_write(a, i); } };
 struct FBceCount { BceArgs a; HD void operator()(u32 i) const { k_bce_count(a, i); } };
@@ -303,7 +301,6 @@ struct pf_sigma_ctx {
     u64 kbytes[K_COUNT] = {};
     u64 phase_ws = 0;  // elected lists' working set of the current phase
     u32 mis_rounds = 0;
-    int bve_mode = 2;  // BVE decision: 0 thread per variable from HBM, 1 thread on a smem copy, 2 warp per variable
 
     Ctx view() {
         Ctx c;
@@ -919,7 +916,7 @@ struct pf_sigma_ctx {
         a.scr_off = ve_scr_off.p;
         a.scr = ve_scr.p;
 #if SIGMA_CUDA
-        if (bve_mode == 2) {
+        {
             const int smem = kBveWarpThreads / 32 * (int)WPV_WORDS * 4;
             static bool attr_set = false;
             if (!attr_set) {
@@ -932,25 +929,10 @@ struct pf_sigma_ctx {
             bve_warp_k<<<(u32)rt.sms * 8u, kBveWarpThreads, smem, rt.stream>>>(a, pv_perm.p, counters.p + 11);
             kclock[K_BVE].stop(rt);
             ck(cudaGetLastError(), "launch");
-        } else if (bve_mode == 1) {
-            const int smem = kBveThreads * (int)PV_SLOT * 4;
-            static bool attr_set = false;
-            if (!attr_set) {
-                ck(cudaFuncSetAttribute(bve_analyze_k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "smem attr");
-                attr_set = true;
-            }
-            ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
-            rt.launches++;
-            bve_analyze_k<<<(u32)rt.sms * 3u, kBveThreads, smem, rt.stream>>>(a, pv_perm.p, counters.p + 11);
-            ck(cudaGetLastError(), "launch");
-        } else {
-            pv_each(FBveAnalyze{a});
         }
 #else
         kclock[K_BVE].start(rt);
-        if (bve_mode == 2) pv_each(FBveWarp{a});
-        else if (bve_mode == 1) pv_each(FBveAnalyzeStaged{a});
-        else pv_each(FBveAnalyze{a});
+        pv_each(FBveWarp{a});
         kclock[K_BVE].stop(rt);
 #endif
         kbytes[K_BVE] += phase_ws;
@@ -1504,7 +1486,6 @@ pf_status pf_sigma_create(const pf_options* opts, pf_sigma_ctx** out) {
         }
         c->rt.init();
         c->tm.init();
-        if (const char* e = std::getenv("SIGMA_BVE_MODE")) c->bve_mode = e[0] - '0';
         c->counters.reserve(c->rt, 32);
         c->counters64.reserve(c->rt, 8);
         c->rt.zero(c->counters.p, 32 * 4);
