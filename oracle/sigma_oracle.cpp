@@ -1197,3 +1197,42 @@ extern "C" long oracle_check_introsort(uint64_t seed, int trials) {
     }
     return bad;
 }
+
+// ---------------------------------------------------------------- model extension
+// MODEL::extend (src/cpu/model.cpp:104-138) over a witness stack, then a count of
+// the clauses of (lits, offsets) that the extended model falsifies. value[v] is 1
+// for true; the stack is walked from its end: a record [first, ..., last, length]
+// whose literals after the first are all false sets its first literal true.
+extern "C" long oracle_extend_and_check(uint32_t num_vars, uint8_t* value, const uint32_t* resolved, uint64_t nres,
+                                        const uint32_t* lits, const uint64_t* offsets, uint64_t num_clauses) {
+    auto sat = [&](uint32_t lit) { return value[lit >> 1] == ((lit & 1u) ? 0 : 1); };
+    if (nres) {
+        uint64_t x = nres - 1;  // the last record's length word
+        while (true) {
+            const uint64_t k = resolved[x];
+            if (k == 0 || k > x) return -1;  // malformed stack
+            const uint64_t first = x - k;
+            bool unsat = true;
+            for (uint64_t j = x - 1; j > first; j--) {
+                if (sat(resolved[j])) {
+                    unsat = false;
+                    break;
+                }
+            }
+            if (unsat) {
+                const uint32_t lit = resolved[first];
+                if ((lit >> 1) > num_vars) return -1;
+                value[lit >> 1] = (lit & 1u) ? 0 : 1;
+            }
+            if (first == 0) break;
+            x = first - 1;
+        }
+    }
+    long bad = 0;
+    for (uint64_t c = 0; c < num_clauses; c++) {
+        bool ok = false;
+        for (uint64_t i = offsets[c]; i < offsets[c + 1] && !ok; i++) ok = sat(lits[i]);
+        bad += !ok;
+    }
+    return bad;
+}

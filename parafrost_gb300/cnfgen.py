@@ -136,14 +136,8 @@ def random_mixed_ksat(num_clauses: int, ratio: float, kmin: int = 2, kmax: int =
     return num_vars, lits, off
 
 
-def aig_tseitin(num_inputs: int = 50_000, num_and: int = 2_000_000, num_xor: int = 200_000,
-                window: float = 0.10, seed: int = 1) -> tuple:
-    """Tseitin encoding of a seeded random and-inverter graph with XOR gates.
-
-    Node n (variables 1..num_inputs are primary inputs) takes two distinct fan-in
-    nodes from the most recent ``window`` fraction of nodes before it, each with a
-    random polarity. AND: (-g a)(-g b)(g -a -b); XOR: (-g a b)(-g -a -b)(g -a b)(g a -b).
-    """
+def _aig_structure(num_inputs: int, num_and: int, num_xor: int, window: float, seed: int) -> tuple:
+    """Gate nodes, fan-in nodes with polarities, and XOR flags of the random AIG."""
     st = Stream(seed, 2)
     num_gates = num_and + num_xor
     num_vars = num_inputs + num_gates
@@ -163,6 +157,20 @@ def aig_tseitin(num_inputs: int = 50_000, num_and: int = 2_000_000, num_xor: int
     # choose exactly num_xor XOR positions: rank gates by a random key
     key = st.u64(num_gates)
     is_xor[np.argsort(key, kind="stable")[:num_xor]] = True
+    return g, a, b, pa, pb, is_xor
+
+
+def aig_tseitin(num_inputs: int = 50_000, num_and: int = 2_000_000, num_xor: int = 200_000,
+                window: float = 0.10, seed: int = 1) -> tuple:
+    """Tseitin encoding of a seeded random and-inverter graph with XOR gates.
+
+    Node n (variables 1..num_inputs are primary inputs) takes two distinct fan-in
+    nodes from the most recent ``window`` fraction of nodes before it, each with a
+    random polarity. AND: (-g a)(-g b)(g -a -b); XOR: (-g a b)(-g -a -b)(g -a b)(g a -b).
+    """
+    g, a, b, pa, pb, is_xor = _aig_structure(num_inputs, num_and, num_xor, window, seed)
+    num_gates = num_and + num_xor
+    num_vars = num_inputs + num_gates
     la = (a << 1) | pa
     lb = (b << 1) | pb
     lg = g << 1
@@ -334,6 +342,29 @@ def community(num_vars: int = 20_000_000, num_clauses: int = 80_000_000, communi
     lits = np.concatenate(lits_parts)
     off = np.concatenate([[0], np.cumsum(np.concatenate(sizes_parts))]).astype(np.uint64)
     return num_vars, lits, off
+
+
+def community_planted(num_vars: int = 20_000_000, seed: int = 1) -> np.ndarray:
+    """The assignment ``community(..., plant=True)`` plants (uint8 per variable,
+    1 = true, index 0 unused): the first draw of the generator's stream."""
+    return Stream(seed, 3).below(2, num_vars + 1).astype(np.uint8)
+
+
+def aig_model(num_inputs: int = 50_000, num_and: int = 2_000_000, num_xor: int = 200_000,
+              window: float = 0.10, seed: int = 1, input_seed: int = 7) -> np.ndarray:
+    """A satisfying assignment of ``aig_tseitin`` with the same arguments: seeded
+    random inputs, every gate evaluated in order (uint8 per variable, 1 = true)."""
+    g, a, b, pa, pb, is_xor = _aig_structure(num_inputs, num_and, num_xor, window, seed)
+    val = np.zeros(num_inputs + num_and + num_xor + 1, dtype=np.uint8)
+    val[1:num_inputs + 1] = Stream(input_seed, 9).below(2, num_inputs).astype(np.uint8)
+    av, bv, xv = a.tolist(), b.tolist(), is_xor.tolist()
+    pav, pbv = pa.tolist(), pb.tolist()
+    vl = val.tolist()
+    for t, node in enumerate(g.tolist()):
+        x = vl[av[t]] ^ (1 if pav[t] else 0)
+        y = vl[bv[t]] ^ (1 if pbv[t] else 0)
+        vl[node] = (x ^ y) if xv[t] else (x & y)
+    return np.array(vl, dtype=np.uint8)
 
 
 def batch_ksat(num_formulas: int = 4096, cmin: int = 1_000, cmax: int = 200_000, seed: int = 1):

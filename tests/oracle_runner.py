@@ -34,7 +34,44 @@ def oracle_lib():
         _lib.oracle_sigmify.argtypes = [
             ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
             ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        _lib.oracle_extend_and_check.restype = ctypes.c_long
+        _lib.oracle_extend_and_check.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
     return _lib
+
+
+def check_models(num_vars, lits, offsets, status, res, model) -> list:
+    """Properties of a simplified formula for a model of the original (uint8 per
+    variable, 1 = true): every surviving clause and every unit holds under it (they
+    are all implied by the original), and the model restricted to the variables that
+    were not eliminated, extended through the witness stack as MODEL::extend does,
+    satisfies every original clause. Returns the failures found (empty = none)."""
+    fails = []
+    if status != 0:
+        return ["round reported UNSAT for a satisfiable formula"]
+    model = np.ascontiguousarray(model, dtype=np.uint8)
+    truth = model[res.lits >> 1] == (1 - (res.lits & 1)).astype(np.uint8)
+    o = res.offsets.astype(np.int64)
+    if o.size > 1:
+        nonempty = o[1:] > o[:-1]
+        if not nonempty.all():
+            fails.append("empty clause in the result")
+        sat = np.logical_or.reduceat(truth, o[:-1][nonempty]) if truth.size else np.zeros(0, bool)
+        if not sat.all():
+            fails.append(f"{int((~sat).sum())} result clauses false under the original's model")
+    u = res.units
+    if u.size and not (model[u >> 1] == (1 - (u & 1))).all():
+        fails.append("a unit is false under the original's model")
+    v = model.copy()
+    v[np.asarray(res.eliminated, dtype=bool)] = 0
+    lits = np.ascontiguousarray(lits, dtype=np.uint32)
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+    resolved = np.ascontiguousarray(res.resolved, dtype=np.uint32)
+    bad = oracle_lib().oracle_extend_and_check(num_vars, v.ctypes.data, resolved.ctypes.data, resolved.size,
+                                               lits.ctypes.data, offsets.ctypes.data, offsets.size - 1)
+    if bad != 0:
+        fails.append(f"extended model falsifies {bad} original clauses" if bad > 0 else "malformed witness stack")
+    return fails
 
 
 def run_oracle(num_vars, lits, offsets, opts: Options | None = None, level: int = 2, learnt=None):
