@@ -20,7 +20,8 @@ constexpr u32 WPV_KC = 64;   // clauses per variable (both lists)
 constexpr u32 WPV_KL = 384;  // literals per variable
 constexpr u32 WPV_XL = 24;   // XOR literal set (arity <= 20)
 // words per warp slot
-constexpr u32 WPV_WORDS = 5 * WPV_KC + WPV_KL + (WPV_KC + 2) + 3 * WPV_XL + 8;
+constexpr u32 WPV_HIST = 16;  // original clauses per size (< 16) per list, counted when staging
+constexpr u32 WPV_WORDS = 5 * WPV_KC + WPV_KL + (WPV_KC + 2) + 3 * WPV_XL + 8 + 2 * WPV_HIST;
 
 struct WarpPv {
     const Ctx* c;
@@ -36,6 +37,7 @@ struct WarpPv {
     u32* xs0;   // list sizes of the XOR literals as staged
     u32* xs1;   // list sizes of their complements
     u32* ctl;
+    u32* hist;  // [side * WPV_HIST + size]
 
     HD void bind(const Ctx& cc, u32* slot) {
         c = &cc;
@@ -50,7 +52,10 @@ struct WarpPv {
         xs0 = xl + WPV_XL;
         xs1 = xs0 + WPV_XL;
         ctl = xs1 + WPV_XL;
+        hist = ctl + 8;
     }
+    // original clauses of `size` in one side's list (sizes >= WPV_HIST: the list length)
+    HD u32 count_size(u32 side, u32 size) const { return size < WPV_HIST ? hist[side * WPV_HIST + size] : n(side); }
     HD u32 n(u32 side) const { return side ? nn : np; }
     HD u32 base(u32 side) const { return side ? np : 0u; }
     HD const u32* L(u32 i) const { return lits + start[i]; }
@@ -69,6 +74,7 @@ HD bool wpv_stage(WarpPv& w, const Ctx& c, u32 var) {
     const u32* lp = c.ot_refs + c.ot_off[p];
     const u32* ln = c.ot_refs + c.ot_off[p + 1];
     const u32 np = w.np;
+    wfor(2 * WPV_HIST, [&](u32 i) { w.hist[i] = 0; });
     wfor(tot, [&](u32 i) {
         const u32 r = i < np ? lp[i] : ln[i - np];
         const Hdr h = c.hdr[r];
@@ -76,6 +82,7 @@ HD bool wpv_stage(WarpPv& w, const Ctx& c, u32 var) {
         w.size[i] = h.size;
         w.sig[i] = h.sig;
         w.flags[i] = h.flags;
+        if (h_original(h.flags) && h.size < WPV_HIST) atom_add(&w.hist[(i < np ? 0u : WPV_HIST) + h.size], 1u);
     });
     wfor(tot, [&](u32 i) {
         u32 s = 0;
@@ -279,6 +286,9 @@ HD bool wpv_ite_pair(const WarpPv& w, u32 dx, u32 i, u32 j, u32& d1, u32& d2) {
 // find_ITE_gate (ifthenelse.h:42-97): first successful pair in (i, j) order.
 HD bool wpv_find_ite_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& nAdded, u32& nLits) {
     const u32 side = dx & 1u, b = w.base(side), ns = w.n(side);
+    // a gate needs a pair of original ternary clauses in this list; without one the
+    // search below fails with no effect
+    if (w.count_size(side, 3) < 2) return false;
     for (u32 a = 0; a < ns; a++) {
         const u32 i = b + a;
         if (!(h_original(w.flags[i]) && w.size[i] == 3)) continue;
@@ -358,12 +368,21 @@ HD bool wpv_find_xor_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& 
     auto freeze_arities = [&]() {
         wpv_unmelt_if(w, 0, w.np + w.nn, [&](u32 i) { return w.size[i] > 2; });
     };
+    // An XOR of arity k has 2^k clauses of size k+1, half of them in each list. A
+    // candidate whose size has fewer originals than that in either list cannot
+    // complete; its search would only melt and then unmelt clauses longer than two,
+    // which freeze_arities does directly.
     for (u32 a = 0; a < ns; a++) {
         const u32 i = b + a;
         if (!h_original(w.flags[i])) continue;
         const u32 size = w.size[i];
         const int arity = (int)size - 1;
         if (size < 3 || arity > o.xor_max_arity) continue;
+        const u32 need = arity - 1 < 31 ? (1u << (arity - 1)) : 0xFFFFFFFFu;
+        if (w.count_size(side, size) < need || w.count_size(side ^ 1u, size) < need) {
+            freeze_arities();
+            continue;
+        }
         wfor(size, [&](u32 k) {
             const u32 lit = w.L(i)[k];
             w.xl[k] = lit;
