@@ -75,27 +75,68 @@ HD bool wpv_stage(WarpPv& w, const Ctx& c, u32 var) {
     const u32* ln = c.ot_refs + c.ot_off[p + 1];
     const u32 np = w.np;
     wfor(2 * WPV_HIST, [&](u32 i) { w.hist[i] = 0; });
-    wfor(tot, [&](u32 i) {
+#if defined(__CUDA_ARCH__)
+    // lane l stages clauses l and l + 32 (tot <= 64): headers, the exclusive prefix
+    // of the sizes by a warp scan, then the literals from the starts kept in registers
+    static_assert(WPV_KC <= 64, "two clauses per lane");
+    const u32 lane = threadIdx.x & 31u;
+    u32 gstart[2] = {0, 0}, carry = 0;
+#pragma unroll
+    for (u32 rr = 0; rr < 2; rr++) {
+        const u32 i = rr * 32u + lane;
+        u32 sz = 0;
+        if (i < tot) {
+            const u32 r = i < np ? lp[i] : ln[i - np];
+            const Hdr h = c.hdr[r];
+            w.id[i] = r;
+            w.size[i] = h.size;
+            w.sig[i] = h.sig;
+            w.flags[i] = h.flags;
+            gstart[rr] = h.start;
+            sz = h.size;
+            if (h_original(h.flags) && h.size < WPV_HIST) atomicAdd(&w.hist[(i < np ? 0u : WPV_HIST) + h.size], 1u);
+        }
+        u32 incl = sz;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 t = __shfl_up_sync(kFull, incl, o);
+            if ((int)lane >= o) incl += t;
+        }
+        if (i < tot) w.start[i] = carry + incl - sz;
+        carry += __shfl_sync(kFull, incl, 31);
+    }
+    __syncwarp();
+    if (carry > WPV_KL) return false;
+#pragma unroll
+    for (u32 rr = 0; rr < 2; rr++) {
+        const u32 i = rr * 32u + lane;
+        if (i < tot) {
+            const u32* src = c.lits + gstart[rr];
+            u32* dst = w.lits + w.start[i];
+            for (u32 k = 0; k < w.size[i]; k++) dst[k] = src[k];
+        }
+    }
+    __syncwarp();
+#else
+    u32 total = 0;
+    for (u32 i = 0; i < tot; i++) {
         const u32 r = i < np ? lp[i] : ln[i - np];
         const Hdr h = c.hdr[r];
         w.id[i] = r;
         w.size[i] = h.size;
         w.sig[i] = h.sig;
         w.flags[i] = h.flags;
-        if (h_original(h.flags) && h.size < WPV_HIST) atom_add(&w.hist[(i < np ? 0u : WPV_HIST) + h.size], 1u);
-    });
-    wfor(tot, [&](u32 i) {
-        u32 s = 0;
-        for (u32 j = 0; j < i; j++) s += w.size[j];
-        w.start[i] = s;
-    });
-    const u32 total = tot ? w.start[tot - 1] + w.size[tot - 1] : 0u;
+        w.start[i] = total;
+        total += h.size;
+        if (h_original(h.flags) && h.size < WPV_HIST) w.hist[(i < np ? 0u : WPV_HIST) + h.size]++;
+    }
     if (total > WPV_KL) return false;
-    wfor(tot, [&](u32 i) {
+    for (u32 i = 0; i < tot; i++) {
         const u32* src = c.lits + c.hdr[w.id[i]].start;
         u32* dst = w.lits + w.start[i];
         for (u32 k = 0; k < w.size[i]; k++) dst[k] = src[k];
-    });
+    }
+#endif
     return true;
 }
 
@@ -371,7 +412,8 @@ HD bool wpv_find_xor_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& 
     // An XOR of arity k has 2^k clauses of size k+1, half of them in each list. A
     // candidate whose size has fewer originals than that in either list cannot
     // complete; its search would only melt and then unmelt clauses longer than two,
-    // which freeze_arities does directly.
+    // which freeze_arities does directly (once while nothing melts in between).
+    bool frozen = false;
     for (u32 a = 0; a < ns; a++) {
         const u32 i = b + a;
         if (!h_original(w.flags[i])) continue;
@@ -380,9 +422,11 @@ HD bool wpv_find_xor_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& 
         if (size < 3 || arity > o.xor_max_arity) continue;
         const u32 need = arity - 1 < 31 ? (1u << (arity - 1)) : 0xFFFFFFFFu;
         if (w.count_size(side, size) < need || w.count_size(side ^ 1u, size) < need) {
-            freeze_arities();
+            if (!frozen) freeze_arities();  // a repeat would change nothing
+            frozen = true;
             continue;
         }
+        frozen = false;  // this candidate's search melts clauses
         wfor(size, [&](u32 k) {
             const u32 lit = w.L(i)[k];
             w.xl[k] = lit;
