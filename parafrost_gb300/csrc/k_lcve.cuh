@@ -360,8 +360,48 @@ __global__ void __launch_bounds__(256) mis_waves_k(LcveArgs a, MisWaves w) {
                 mis_push_clause(a, u, ru, uin, hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])]), app);
             __syncwarp();
         }
+        // small vertices: a warp takes 32 of them and spreads all their clauses over
+        // its lanes (a prefix of the clause counts maps each lane's clause to its
+        // vertex), so every lane walks about as many clauses as the others
         const u32* in_s = w.small[wave & 1];
-        for (u32 idx = tid; idx < ns; idx += nth) mis_push_vertex(a, vload(&in_s[idx]), app);
+        for (u32 base = (tid >> 5) * 32u; base < ns; base += nwarps * 32u) {
+            const u32 idx = base + lane;
+            const u32 u = idx < ns ? vload(&in_s[idx]) : 0u;
+            const u64 wu = u ? vload64(&a.word[u]) : 0ull;
+            const u32 p = V2L(u);
+            const u32 np = u ? a.c.ot_size[p] : 0u, cnt = u ? np + a.c.ot_size[p + 1] : 0u;
+            const u32 op = u ? a.c.ot_off[p] : 0u, on = u ? a.c.ot_off[p + 1] : 0u;
+            u32 incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const u32 t = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)lane >= o) incl += t;
+            }
+            const u32 start = incl - cnt;
+            const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+            for (u32 t0 = 0; t0 < total; t0 += 32u) {
+                const u32 t = t0 + lane;
+                // owner: the last lane whose start is <= t
+                u32 lo = 0;
+#pragma unroll
+                for (u32 step = 16; step; step >>= 1) {
+                    const u32 s_mid = __shfl_sync(0xffffffffu, start, (int)(lo + step));
+                    if (lo + step < 32u && s_mid <= t) lo += step;
+                }
+                const u32 ou = __shfl_sync(0xffffffffu, u, (int)lo);
+                const u64 owu = __shfl_sync(0xffffffffu, wu, (int)lo);
+                const u32 onp = __shfl_sync(0xffffffffu, np, (int)lo);
+                const u32 oop = __shfl_sync(0xffffffffu, op, (int)lo);
+                const u32 oon = __shfl_sync(0xffffffffu, on, (int)lo);
+                const u32 ost = __shfl_sync(0xffffffffu, start, (int)lo);
+                if (t < total) {
+                    const u32 k = t - ost;
+                    const u32 r = ldro(&a.c.ot_refs[k < onp ? oop + k : oon + (k - onp)]);
+                    mis_push_clause(a, ou, mis_rank(owu), mis_dec(owu) == MIS_IN, hdr_ro(&a.c.hdr[r]), app);
+                }
+                __syncwarp();
+            }
+        }
         mis_queue_flush(q, f);
         if (!grid_barrier(w.bar, a.c.err)) return;
     }
