@@ -247,6 +247,60 @@ HD void k_mis_push(const LcveArgs& a, const u32* in, const MisFront& f, u32 idx)
     });
 }
 #else
+// Count for the small graph vertices with a warp per 32 consecutive variables: the
+// clauses of the 32 are spread over the lanes (as in the waves), each lane adds its
+// clauses' lower-neighbour occurrences to the owner's counter in shared memory.
+__global__ void __launch_bounds__(256) mis_count_flat_k(LcveArgs a, MisFront f, u32 nvars) {
+    __shared__ u32 acc[8][32];
+    const u32 lane = threadIdx.x & 31u, wl = threadIdx.x >> 5;
+    const u32 nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (u32 base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; base <= nvars; base += nwarps * 32u) {
+        const u32 v = base + lane;
+        const u64 wv = (v && v <= nvars) ? a.word[v] : (u64)NONE;
+        const bool counted = mis_rank(wv) != NONE && !mis_is_big(a.c, v);
+        const u32 p = V2L(v);
+        const u32 np = counted ? a.c.ot_size[p] : 0u, cnt = counted ? np + a.c.ot_size[p + 1] : 0u;
+        const u32 op = counted ? a.c.ot_off[p] : 0u, on = counted ? a.c.ot_off[p + 1] : 0u;
+        u64 ws = 4ull * cnt;
+        acc[wl][lane] = 0;
+        u32 incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 t = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o) incl += t;
+        }
+        const u32 start = incl - cnt;
+        const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        for (u32 t0 = 0; t0 < total; t0 += 32u) {
+            const u32 t = t0 + lane;
+            u32 lo = 0;
+#pragma unroll
+            for (u32 step = 16; step; step >>= 1) {
+                const u32 s_mid = __shfl_sync(0xffffffffu, start, (int)(lo + step));
+                if (lo + step < 32u && s_mid <= t) lo += step;
+            }
+            const u32 ov = __shfl_sync(0xffffffffu, v, (int)lo);
+            const u64 owv = __shfl_sync(0xffffffffu, wv, (int)lo);
+            const u32 onp = __shfl_sync(0xffffffffu, np, (int)lo);
+            const u32 oop = __shfl_sync(0xffffffffu, op, (int)lo);
+            const u32 oon = __shfl_sync(0xffffffffu, on, (int)lo);
+            const u32 ost = __shfl_sync(0xffffffffu, start, (int)lo);
+            if (t < total) {
+                const u32 k = t - ost;
+                const u32 r = ldro(&a.c.ot_refs[k < onp ? oop + k : oon + (k - onp)]);
+                const u32 nl = mis_lower_in_hdr(a, ov, mis_rank(owv), hdr_ro(&a.c.hdr[r]), ws);
+                if (nl) atomicAdd(&acc[wl][lo], nl);
+            }
+        }
+        __syncwarp();
+        const bool in0 = counted && mis_set_count(a, v, mis_rank(wv), acc[wl][lane]);
+        mis_append(f, a.c, v, in0);
+        warp_sum_add64(a.ws_bytes, ws);
+        __syncwarp();
+    }
+}
+
 // Count for the large graph vertices, one warp each (lanes take its clauses). The
 // list length is read from device memory (no host round trip).
 __global__ void mis_count_warp_k(LcveArgs a, const u32* in, const u32* n_ptr, MisFront f) {

@@ -46,7 +46,9 @@ struct FReduce { Ctx c; HD void operator()(u32 i) const { k_reduce_list(c, i); }
 struct FScores { LcveArgs a; u32* max_score; HD void operator()(u32 i) const { k_scores(a, max_score, i); } };
 struct FRank { LcveArgs a; HD void operator()(u32 i) const { k_rank(a, i); } };
 struct FMisInit { LcveArgs a; MisFront b; HD void operator()(u32 i) const { k_mis_init(a, b, i); } };
+#if !SIGMA_CUDA
 struct FMisCount { LcveArgs a; MisFront f; HD void operator()(u32 i) const { k_mis_count(a, f, i); } };
+#endif
 #if !SIGMA_CUDA
 struct FMisPush { LcveArgs a; const u32* in; MisFront f; HD void operator()(u32 i) const { k_mis_push(a, in, f, i); } };
 struct FMisCountBig { LcveArgs a; const u32* in; MisFront f; HD void operator()(u32 i) const { k_mis_count_big(a, in, f, i); } };
@@ -633,10 +635,11 @@ struct pf_sigma_ctx {
         rt.zero(ctr, 9 * 4);
         rt.each(FMisInit{a, MisFront{nullptr, nullptr, mis_big_b.p, ctr + 3}}, nvars + 1);
         MisFront f0{flags.p, ctr, mis_big_a.p, ctr + 1};
-        rt.each(FMisCount{a, f0}, nvars + 1);
         u32 rounds = 0;
 #if SIGMA_CUDA
-        rt.launches += 2;
+        rt.launches += 3;
+        mis_count_flat_k<<<rt.grid(nvars + 1, 8), 256, 0, rt.stream>>>(a, f0, nvars);
+        ck(cudaGetLastError(), "launch");
         mis_count_warp_k<<<rt.sms * 8, 256, 0, rt.stream>>>(a, mis_big_b.p, ctr + 3, f0);
         ck(cudaGetLastError(), "launch");
         MisWaves w;
@@ -658,6 +661,7 @@ struct pf_sigma_ctx {
         check();
         rounds = read_u32(ctr + 8);
 #else
+        rt.each(FMisCount{a, f0}, nvars + 1);
         rt.each(FMisCountBig{a, mis_big_b.p, f0}, read_u32(ctr + 3));
         MisFront fin = f0;
         MisFront fout{flags_scan.p, ctr + 2, mis_big_b.p, ctr + 3};
