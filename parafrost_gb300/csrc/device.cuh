@@ -295,6 +295,24 @@ HD int popc32(u32 x) {
 #endif
 }
 
+// Four words in one 16-byte load (usable in host and device code alike).
+struct __align__(16) Q4 {
+    u32 x, y, z, w;
+};
+HD Q4 ldro4(const Q4* p) {
+#if defined(__CUDA_ARCH__)
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+    Q4 q;
+    q.x = v.x;
+    q.y = v.y;
+    q.z = v.z;
+    q.w = v.w;
+    return q;
+#else
+    return *p;
+#endif
+}
+
 // Pair of words (usable in host and device code alike).
 struct U2 {
     u32 x, y;

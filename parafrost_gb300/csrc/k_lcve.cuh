@@ -37,6 +37,7 @@ struct LcveArgs {
     u32* order;           // nvars: variables in (score, var) order
     u32* rank;            // nvars+1
     u64* word;            // nvars+1: independent-set words
+    const Q4* crec;       // per clause: its first three literals and size | deleted << 31
     u64* ws_bytes;        // accumulates the graph's working set (4*occ + sum(8 + 4*len))
     u32* bound;           // per formula f: [2f] = B0 (first valid non-F rank), [2f+1] = B
     const u32* f_active;  // batches: formulas taking part in this election (null: all)
@@ -115,24 +116,59 @@ HD void k_mis_init(const LcveArgs& a, const MisFront& bigs, u32 v) {
 // while the independent set is decided.
 constexpr u32 MIS_CHUNK = 4;
 
+// A clause as the election reads it: one 16-byte record holding its first three
+// literals and its size and deleted bit (built once per election by k_mis_rec), so
+// clauses of up to three literals cost one load; longer ones read the rest of
+// their literals from the store.
+HD void k_mis_rec(const Ctx& c, Q4* rec, u32 i) {
+    const Hdr h = c.hdr[i];
+    const u32* l = c.lits + h.start;
+    Q4 q;
+    q.x = h.size > 0 ? l[0] : 0u;
+    q.y = h.size > 1 ? l[1] : 0u;
+    q.z = h.size > 2 ? l[2] : 0u;
+    q.w = h.size | (h_deleted(h.flags) ? 0x80000000u : 0u);
+    rec[i] = q;
+}
+struct MisCl {
+    Q4 q;
+    u32 r;
+    HD bool deleted() const { return (q.w >> 31) != 0; }
+    HD u32 size() const { return q.w & 0x7FFFFFFFu; }
+};
+HD MisCl mis_cl(const LcveArgs& a, u32 r) {
+    MisCl cl;
+    cl.q = ldro4(&a.crec[r]);
+    cl.r = r;
+    return cl;
+}
+// Literal k of the clause; L is the clause's literal array (read only for k >= 3).
+HD u32 mis_lit(const MisCl& cl, const u32* L, u32 k) {
+    return k == 0 ? cl.q.x : k == 1 ? cl.q.y : k == 2 ? cl.q.z : ldro(L + k);
+}
+HD const u32* mis_long_lits(const LcveArgs& a, const MisCl& cl) {
+    return cl.size() > 3 ? a.c.lits + hdr_ro(&a.c.hdr[cl.r]).start : nullptr;
+}
+
 // Occurrences of graph vertices ranked below rv (other than v) in clause r, and
 // the clause's bytes (8 + 4*len when live) added to ws.
-HD u32 mis_lower_in_hdr(const LcveArgs& a, u32 v, u32 rv, const Hdr& h, u64& ws) {
-    if (h_deleted(h.flags)) return 0;
-    ws += 8ull + 4ull * h.size;
-    const u32* L = a.c.lits + h.start;
+HD u32 mis_lower_in_hdr(const LcveArgs& a, u32 v, u32 rv, const MisCl& cl, u64& ws) {
+    if (cl.deleted()) return 0;
+    const u32 size = cl.size();
+    ws += 8ull + 4ull * size;
+    const u32* L = mis_long_lits(a, cl);
     u32 n = 0;
-    for (u32 k0 = 0; k0 < h.size; k0 += MIS_CHUNK) {
+    for (u32 k0 = 0; k0 < size; k0 += MIS_CHUNK) {
         u32 w[MIS_CHUNK];
 #pragma unroll
-        for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < h.size ? ABS(ldro(L + k0 + j)) : v;
+        for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < size ? ABS(mis_lit(cl, L, k0 + j)) : v;
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) n += (w[j] != v && mis_rank(a.word[w[j]]) < rv) ? 1u : 0u;
     }
     return n;
 }
 HD u32 mis_lower_in_clause(const LcveArgs& a, u32 v, u32 rv, u32 r, u64& ws) {
-    return mis_lower_in_hdr(a, v, rv, hdr_ro(&a.c.hdr[r]), ws);
+    return mis_lower_in_hdr(a, v, rv, mis_cl(a, r), ws);
 }
 
 // Stores the lower-neighbour count of graph vertex v; a vertex with none goes in
@@ -155,10 +191,10 @@ HD bool mis_count_one(const LcveArgs& a, u32 v, u64& ws) {
     ws += 4ull * n_all;
     u32 n = 0;
     if (n_all) {
-        Hdr h = hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[op])]);
+        MisCl h = mis_cl(a, ldro(&a.c.ot_refs[op]));
         for (u32 t = 0; t < n_all; t++) {
-            Hdr hn = h;
-            if (t + 1 < n_all) hn = hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1])]);
+            MisCl hn = h;
+            if (t + 1 < n_all) hn = mis_cl(a, ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1]));
             n += mis_lower_in_hdr(a, v, rv, h, ws);
             h = hn;
         }
@@ -182,15 +218,16 @@ HD void k_mis_count(const LcveArgs& a, const MisFront& f, u32 v) {
 // push that takes a count from one to zero marks that neighbour in: no other push
 // can reach it any more.
 template <class App>
-HD void mis_push_clause(const LcveArgs& a, u32 u, u32 ru, bool in, const Hdr& h, App app) {
-    if (h_deleted(h.flags)) return;
-    const u32* L = a.c.lits + h.start;
-    for (u32 k0 = 0; k0 < h.size; k0 += MIS_CHUNK) {
+HD void mis_push_clause(const LcveArgs& a, u32 u, u32 ru, bool in, const MisCl& cl, App app) {
+    if (cl.deleted()) return;
+    const u32 size = cl.size();
+    const u32* L = mis_long_lits(a, cl);
+    for (u32 k0 = 0; k0 < size; k0 += MIS_CHUNK) {
         u32 w[MIS_CHUNK];
         u64 old[MIS_CHUNK];
         bool up[MIS_CHUNK];
 #pragma unroll
-        for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < h.size ? ABS(ldro(L + k0 + j)) : u;
+        for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < size ? ABS(mis_lit(cl, L, k0 + j)) : u;
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) {
             const u32 g = w[j] != u ? mis_rank(a.word[w[j]]) : NONE;
@@ -222,10 +259,10 @@ HD void mis_push_vertex(const LcveArgs& a, u32 u, App app) {
     const u32 p = V2L(u), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
     const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
     if (!n) return;
-    Hdr h = hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[op])]);
+    MisCl h = mis_cl(a, ldro(&a.c.ot_refs[op]));
     for (u32 t = 0; t < n; t++) {
-        Hdr hn = h;
-        if (t + 1 < n) hn = hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1])]);
+        MisCl hn = h;
+        if (t + 1 < n) hn = mis_cl(a, ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1]));
         mis_push_clause(a, u, ru, in, h, app);
         h = hn;
     }
@@ -289,7 +326,7 @@ __global__ void __launch_bounds__(256) mis_count_flat_k(LcveArgs a, MisFront f, 
             if (t < total) {
                 const u32 k = t - ost;
                 const u32 r = ldro(&a.c.ot_refs[k < onp ? oop + k : oon + (k - onp)]);
-                const u32 nl = mis_lower_in_hdr(a, ov, mis_rank(owv), hdr_ro(&a.c.hdr[r]), ws);
+                const u32 nl = mis_lower_in_hdr(a, ov, mis_rank(owv), mis_cl(a, r), ws);
                 if (nl) atomicAdd(&acc[wl][lo], nl);
             }
         }
@@ -411,7 +448,7 @@ __global__ void __launch_bounds__(256) mis_waves_k(LcveArgs a, MisWaves w) {
             const u32 p = V2L(u), np = a.c.ot_size[p], nn = a.c.ot_size[p + 1];
             const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
             for (u32 t = lane; t < np + nn; t += 32)
-                mis_push_clause(a, u, ru, uin, hdr_ro(&a.c.hdr[ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])]), app);
+                mis_push_clause(a, u, ru, uin, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])), app);
             __syncwarp();
         }
         // small vertices: a warp takes 32 of them and spreads all their clauses over
@@ -451,7 +488,7 @@ __global__ void __launch_bounds__(256) mis_waves_k(LcveArgs a, MisWaves w) {
                 if (t < total) {
                     const u32 k = t - ost;
                     const u32 r = ldro(&a.c.ot_refs[k < onp ? oop + k : oon + (k - onp)]);
-                    mis_push_clause(a, ou, mis_rank(owu), mis_dec(owu) == MIS_IN, hdr_ro(&a.c.hdr[r]), app);
+                    mis_push_clause(a, ou, mis_rank(owu), mis_dec(owu) == MIS_IN, mis_cl(a, r), app);
                 }
                 __syncwarp();
             }

@@ -45,6 +45,7 @@ struct FPropClause { PropArgs a; HD void operator()(u32 i) const { k_prop_clause
 struct FReduce { Ctx c; HD void operator()(u32 i) const { k_reduce_list(c, i); } };
 struct FScores { LcveArgs a; u32* max_score; HD void operator()(u32 i) const { k_scores(a, max_score, i); } };
 struct FRank { LcveArgs a; HD void operator()(u32 i) const { k_rank(a, i); } };
+struct FMisRec { Ctx c; Q4* rec; HD void operator()(u32 i) const { k_mis_rec(c, rec, i); } };
 struct FMisInit { LcveArgs a; MisFront b; HD void operator()(u32 i) const { k_mis_init(a, b, i); } };
 #if !SIGMA_CUDA
 struct FMisCount { LcveArgs a; MisFront f; HD void operator()(u32 i) const { k_mis_count(a, f, i); } };
@@ -257,6 +258,7 @@ struct pf_sigma_ctx {
     DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
     DBuf<u32> mis_big_a, mis_big_b;
     DBuf<u64> mis_word;
+    DBuf<Q4> mis_rec;  // the election's 16-byte clause records
     DBuf<u32> pv_perm, pv_key;
     DBuf<u32> work, cl_stamp;
     DBuf<u32> radix_hist, radix_hscan, scan_tmp32;
@@ -607,6 +609,8 @@ struct pf_sigma_ctx {
         a.order = order.p;
         a.rank = rank.p;
         a.word = mis_word.p;
+        mis_rec.reserve(rt, (size_t)ncls + 1);
+        a.crec = mis_rec.p;
         a.ws_bytes = counters64.p + 4;
         a.bound = bound.p;
         a.pvs = pvs.p;
@@ -634,6 +638,7 @@ struct pf_sigma_ctx {
         u32* ctr = counters.p + 12;  // [12..17] frontier lengths, [18..19] barrier, [20] waves
         rt.zero(ctr, 9 * 4);
         rt.each(FMisInit{a, MisFront{nullptr, nullptr, mis_big_b.p, ctr + 3}}, nvars + 1);
+        rt.each(FMisRec{a.c, mis_rec.p}, ncls);
         MisFront f0{flags.p, ctr, mis_big_a.p, ctr + 1};
         u32 rounds = 0;
 #if SIGMA_CUDA
@@ -2065,6 +2070,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     for (auto* b : b64) b->free();
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
     c.mis_word.free();
+    c.mis_rec.free();
     c.res_mark.free();
 #if SIGMA_CUDA
     c.scan1_agg.free();
