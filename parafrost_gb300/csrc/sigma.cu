@@ -89,13 +89,13 @@ struct Perm {
 };
 // Work-order key of elected variable k: descending clause count.
 // Elected variables from n_first on (a batch's stopping formulas) come after the
-// others; clause counts above 2^23 share the first place (24-bit keys).
+// others; clause counts from 127 up share the first place (one 8-bit radix pass).
 struct FPvKey {
     Ctx c; const u32* pvs; u32* key; u32* val; u32 n_first;
     HD void operator()(u32 k) const {
         const u32 p = V2L(pvs[k]);
         const u32 occ = c.ot_size[p] + c.ot_size[p + 1];
-        key[k] = (k >= n_first ? 0x800000u : 0u) | (0x7FFFFFu - (occ < 0x7FFFFFu ? occ : 0x7FFFFFu));
+        key[k] = (k >= n_first ? 0x80u : 0u) | (0x7Fu - (occ < 0x7Fu ? occ : 0x7Fu));
         val[k] = k;
     }
 };
@@ -713,9 +713,9 @@ struct pf_sigma_ctx {
         pv_perm.reserve(rt, nvars + 1);
         pv_key.reserve(rt, nvars + 1);
         rt.each(FPvKey{view(), pvs.p, pv_key.p, pv_perm.p, n_go}, npvs);
-        radix_sort_pairs(pv_key.p, pv_perm.p, order_k2.p, order_v2.p, npvs, 24, radix_hist.p, radix_hscan.p,
+        radix_sort_pairs(pv_key.p, pv_perm.p, order_k2.p, order_v2.p, npvs, 8, radix_hist.p, radix_hscan.p,
                          scan_tmp32.p, rt.stream);
-        rt.launches += 15;
+        rt.launches += 5;
     }
 
     // f(k) for every elected variable, in work order, dynamically scheduled.
