@@ -61,6 +61,39 @@ HD void k_bce_count(const BceArgs& a, u32 k) {
     a.nwit[k] = w;
 }
 
+// Count step with one warp per elected variable: the lanes take the negative
+// clauses, each checking its own against the whole positive list.
+HD void bce_count_warp(const BceArgs& a, u32 k) {
+    const Ctx& c = a.c;
+    const u32 v = a.pvs[k];
+    const u32 p = V2L(v), n = NEG(p);
+    const bool skip = c.vstate[v] || c.ot_size[p] > a.bce_max || c.ot_size[n] > a.bce_max;
+    u32 w = 0;
+    if (!skip) {
+        const ListRef poss = list_of(c, p), negs = list_of(c, n);
+        w = wsum(negs.n, [&](u32 i) {
+            const Hdr neg = c.hdr[negs.ids[i]];
+            return (h_original(neg.flags) && bce_blocked(c, v, neg, poss)) ? neg.size + 1 : 0u;
+        });
+    }
+    wone([&] { a.nwit[k] = w; });
+}
+
+#if SIGMA_CUDA
+// Warps take elected variables in work order (perm), a few at a time.
+__global__ void __launch_bounds__(256) bce_count_warp_k(BceArgs a, const u32* perm, u32 npos, u32* next) {
+    const u32 lane = threadIdx.x & 31u;
+    while (true) {
+        u32 j0 = 0;
+        if (lane == 0) j0 = atomicAdd(next, 4u);
+        j0 = __shfl_sync(0xffffffffu, j0, 0);
+        if (j0 >= npos) break;
+        const u32 j1 = j0 + 4u < npos ? j0 + 4u : npos;
+        for (u32 j = j0; j < j1; j++) bce_count_warp(a, perm[j]);
+    }
+}
+#endif
+
 // Write step: save each blocked clause with witness -v, then delete it.
 HD void k_bce_write(const BceArgs& a, u32 k) {
     const Ctx& c = a.c;

@@ -294,6 +294,103 @@ HD void k_bve_write(const BveArgs& a, u32 k) {
     c.vstate[v] = 1;  // markEliminated (src/cpu/solve.h:535-541)
 }
 
+#if SIGMA_CUDA
+// Step 2 with one warp per elected variable: the resolvent pairs, in the
+// reference's (i, j) order, go over the lanes 32 at a time; a warp prefix of the
+// kept ones gives each its id and literal offset, so the clauses land where the
+// sequential loop puts them. Equivalences and the witness/deletion part run on
+// lane 0 as in k_bve_write.
+__device__ void bve_write_warp(const BveArgs& a, u32 k) {
+    const Ctx& c = a.c;
+    const u32 lane = threadIdx.x & 31u;
+    const uint8_t type = a.type[k];
+    if (type == VE_KEEP) return;
+    if (type == VE_EQU || !a.ncls[k]) {
+        if (lane == 0) k_bve_write(a, k);
+        __syncwarp();
+        return;
+    }
+    const u32 v = a.pvs[k];
+    const u32 p = V2L(v), n = NEG(p);
+    u32 dx = p, fx = n;
+    if (c.ot_size[dx] > c.ot_size[fx]) swap_t(dx, fx);
+    const ListRef me = list_of(c, dx), other = list_of(c, fx);
+    const bool gate = type == VE_SUBST;
+    u32 id = a.cls_base + a.cls_scan[k];
+    u64 ls = a.lit_base + a.lit_scan[k];
+    const u32 id_end = id + a.ncls[k];
+    const u64 ls_end = ls + a.nlits[k];
+    const u32 pairs = me.n * other.n;
+    bool bad = false;
+    for (u32 b0 = 0; b0 < pairs; b0 += 32u) {
+        const u32 q = b0 + lane;
+        int rs = 0;
+        Hdr hi, hj;
+        if (q < pairs) {
+            hi = c.hdr[me.ids[q / other.n]];
+            hj = c.hdr[other.ids[q % other.n]];
+            if (h_original(hi.flags) && h_original(hj.flags) && !(gate && h_molten(hi.flags) == h_molten(hj.flags)))
+                rs = merge_size(v, c.lits + hi.start, hi.size, c.lits + hj.start, hj.size);
+        }
+        if (rs == 1) {
+            u32 buf[1];
+            u32 on = 0;
+            merge_into(v, c.lits + hi.start, hi.size, c.lits + hj.start, hj.size, buf, on);
+            enqueue_unit(c, buf[0]);
+        }
+        const bool keep = rs >= 2;
+        const u32 kept = __ballot_sync(0xffffffffu, keep);
+        u64 lits = keep ? (u64)rs : 0ull;
+        u64 incl = lits;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u64 t = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o) incl += t;
+        }
+        const u32 my_id = id + (u32)__popc(kept & ((1u << lane) - 1u));
+        const u64 my_ls = ls + incl - lits;
+        if (keep) {
+            if (my_id >= id_end || my_ls + lits > ls_end) {
+                bad = true;
+            } else {
+                u32 on = 0;
+                merge_into(v, c.lits + hi.start, hi.size, c.lits + hj.start, hj.size, c.lits + my_ls, on);
+                Hdr nh;
+                nh.start = (u32)my_ls;
+                nh.size = on;
+                nh.sig = calc_sig(c.lits + my_ls, on);
+                nh.flags = ST_ORIGINAL | F_ADDED;
+                c.hdr[my_id] = nh;
+            }
+        }
+        id += (u32)__popc(kept);
+        ls += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    __syncwarp();
+    if (lane == 0) {
+        if (bad || id != id_end || ls != ls_end) set_err(c, ERR_INTERNAL);
+        else {
+            oblivion_var(c, p, a.porgs[k], a.norgs[k], a.wit_base + a.wit_scan[k]);
+            c.vstate[v] = 1;  // markEliminated (src/cpu/solve.h:535-541)
+        }
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(256) bve_write_warp_k(BveArgs a, const u32* perm, u32 npos, u32* next) {
+    const u32 lane = threadIdx.x & 31u;
+    while (true) {
+        u32 j0 = 0;
+        if (lane == 0) j0 = atomicAdd(next, 4u);
+        j0 = __shfl_sync(0xffffffffu, j0, 0);
+        if (j0 >= npos) break;
+        const u32 j1 = j0 + 4u < npos ? j0 + 4u : npos;
+        for (u32 j = j0; j < j1; j++) bve_write_warp(a, perm[j]);
+    }
+}
+#endif
+
 // Per-variable scratch words for the AND/OR fan-in list.
 HD void k_bve_scratch_need(const Ctx& c, const u32* pvs, u64* need, u32 k) {
     const u32 p = V2L(pvs[k]);

@@ -73,6 +73,7 @@ struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) co
 struct FBveWarp { BveArgs a; HD void operator()(u32 i) const { k_bve_warp(a, i); } };
 struct FBveWrite { BveArgs a; HD void operator()(u32 i) const { k_bve_write(a, i); } };
 struct FBceCount { BceArgs a; HD void operator()(u32 i) const { k_bce_count(a, i); } };
+struct FBceCountWarp { BceArgs a; HD void operator()(u32 i) const { bce_count_warp(a, i); } };
 struct FBceWrite { BceArgs a; HD void operator()(u32 i) const { k_bce_write(a, i); } };
 struct FEre { EreArgs a; HD void operator()(u32 i) const { k_ere_pv(a, i); } };
 struct FEreCount { EreArgs a; const u32* perm; u64* cnt; HD void operator()(u32 q) const { k_ere_count(a, perm, cnt, q); } };
@@ -960,7 +961,17 @@ struct pf_sigma_ctx {
         a.lit_base = nlits_used;
         a.wit_base = nresolved;
         kclock[K_BVEW].start(rt);
+#if SIGMA_CUDA
+        if (perm_n) {
+            ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
+            rt.launches++;
+            bve_write_warp_k<<<(u32)rt.sms * 8u, 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n,
+                                                                       counters.p + 11);
+            ck(cudaGetLastError(), "launch");
+        }
+#else
         pv_each(FBveWrite{a});
+#endif
         kclock[K_BVEW].stop(rt);
         kbytes[K_BVEW] += phase_ws + 4ull * add_lits + 8ull * add_cls + 4ull * add_wit;
         ncls += add_cls;
@@ -981,7 +992,16 @@ struct pf_sigma_ctx {
         ve_nwit.reserve(rt, npvs);
         ve_wit_scan.reserve(rt, npvs);
         a.nwit = ve_nwit.p;
-        pv_each(FBceCount{a});
+#if SIGMA_CUDA
+        if (perm_n) {
+            ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
+            rt.launches++;
+            bce_count_warp_k<<<(u32)rt.sms * 8u, 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n, counters.p + 11);
+            ck(cudaGetLastError(), "launch");
+        }
+#else
+        pv_each(FBceCountWarp{a});
+#endif
         const u64 add = scan64(ve_nwit.p, ve_wit_scan.p, npvs);
         if (!add) return;
         ensure_resolved(nresolved + add);
