@@ -43,26 +43,10 @@ HD bool bce_blocked(const Ctx& c, u32 v, const Hdr& neg, const ListRef& poss) {
     return true;
 }
 
-// Count step: witness words of the negative clauses blocked on v.
-HD void k_bce_count(const BceArgs& a, u32 k) {
-    const Ctx& c = a.c;
-    const u32 v = a.pvs[k];
-    a.nwit[k] = 0;
-    if (c.vstate[v]) return;  // eliminated by VE in this phase (PVs[i] == 0)
-    const u32 p = V2L(v), n = NEG(p);
-    if (c.ot_size[p] > a.bce_max || c.ot_size[n] > a.bce_max) return;
-    const ListRef poss = list_of(c, p), negs = list_of(c, n);
-    u32 w = 0;
-    for (u32 i = 0; i < negs.n; i++) {
-        const Hdr neg = c.hdr[negs.ids[i]];
-        if (!h_original(neg.flags)) continue;
-        if (bce_blocked(c, v, neg, poss)) w += neg.size + 1;
-    }
-    a.nwit[k] = w;
-}
-
-// Count step with one warp per elected variable: the lanes take the negative
-// clauses, each checking its own against the whole positive list.
+// Count step (witness words of the negative clauses blocked on v), one warp per
+// elected variable: the lanes take the negative clauses, each checking its own
+// against the whole positive list. A variable eliminated by VE in this phase is
+// skipped (PVs[i] == 0 in the reference).
 HD void bce_count_warp(const BceArgs& a, u32 k) {
     const Ctx& c = a.c;
     const u32 v = a.pvs[k];

@@ -72,7 +72,6 @@ struct FSubAssign { Ctx c; const U2* units; HD void operator()(u32 i) const { en
 struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) const { k_bve_scratch_need(c, pvs, need, i); } };
 struct FBveWarp { BveArgs a; HD void operator()(u32 i) const { k_bve_warp(a, i); } };
 struct FBveWrite { BveArgs a; HD void operator()(u32 i) const { k_bve_write(a, i); } };
-struct FBceCount { BceArgs a; HD void operator()(u32 i) const { k_bce_count(a, i); } };
 struct FBceCountWarp { BceArgs a; HD void operator()(u32 i) const { bce_count_warp(a, i); } };
 struct FBceWrite { BceArgs a; HD void operator()(u32 i) const { k_bce_write(a, i); } };
 struct FEre { EreArgs a; HD void operator()(u32 i) const { k_ere_pv(a, i); } };
