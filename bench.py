@@ -206,7 +206,7 @@ def run_reference(args) -> dict:
 
 
 # Kernel names in the ncu captures summarised under profiles/.
-NCU_NAMES = {"mis_waves": "mis_waves_k", "bve_decide": "bve_warp_k", "sub": "FSubPv", "bve_write": "FBveWrite"}
+NCU_NAMES = {"mis_rounds": "mis_rounds_k", "bve_decide": "bve_warp_k", "sub": "sub_warp_k", "bve_write": "bve_write_warp_k"}
 
 
 def profiled_traffic(kernel: str, workload: str):

@@ -76,10 +76,10 @@ typedef struct {
     double ms_stage[12];      /* ot, prop, lcve, sort, sub, ve, bce, ere, gc, count, upload, download */
     uint64_t algorithmic_bytes; /* bytes the round's kernels must move (HBM roofline numerator) */
     uint32_t kernel_launches;   /* kernels launched by the round */
-    uint32_t mis_rounds;        /* frontier waves of the independent-set elections */
+    uint32_t mis_rounds;        /* push/pull rounds of the independent-set elections */
     uint32_t reserved[2];
     /* The hottest kernels, timed with CUDA events on the context stream:
-     * [0] independent-set waves (LCVE), [1] BVE decision, [2] SUB, [3] BVE write. */
+     * [0] independent-set rounds (LCVE), [1] BVE decision, [2] SUB, [3] BVE write. */
     double ms_kernel[4];        /* device time summed over the round's launches */
     uint64_t bytes_kernel[4];   /* algorithmic bytes those launches processed */
     uint32_t launches_kernel[4];

@@ -18,15 +18,15 @@
 
 namespace sigma {
 
-// Independent-set word of a variable (one 64-bit word, so a neighbour test and its
-// update touch one sector): bits 0-31 the variable's rank if it is a vertex of the
-// graph (NONE otherwise, which never changes while the set is decided), bits 32-61
-// the count of lower-neighbour occurrences not yet out, bits 62-63 the decision.
+// Independent-set word of a variable (one 64-bit word, so a neighbour test reads
+// one sector): bits 0-31 the variable's rank if it is a vertex of the graph (NONE
+// otherwise; never changes while the set is decided), bits 32-61 where the
+// vertex's last pull walk stopped (an index into its two lists), bits 62-63 the
+// decision.
 enum : u32 { MIS_UNDECIDED = 0, MIS_IN = 1, MIS_OUT = 2 };
-constexpr u64 MIS_CNT_ONE = 1ull << 32;
-constexpr u32 MIS_CNT_MAX = (1u << 30) - 1u;
 HD u32 mis_rank(u64 w) { return (u32)w; }
-HD u32 mis_cnt(u64 w) { return (u32)(w >> 32) & MIS_CNT_MAX; }
+HD u32 mis_resume(u64 w) { return (u32)(w >> 32) & 0x3FFFFFFFu; }
+HD u64 mis_with_resume(u32 rank, u32 pos) { return (u64)rank | ((u64)pos << 32); }
 HD u32 mis_dec(u64 w) { return (u32)(w >> 62); }
 HD u64 mis_dec_bits(u32 d) { return (u64)d << 62; }
 
@@ -73,20 +73,24 @@ HD void k_rank(const LcveArgs& a, u32 p) {
     if (lcve_valid(a.c, v) && !lcve_freezable(a, v)) atom_min(&a.bound[2 * fid_of(a.c, v)], p);
 }
 
-// The independent set is decided by pushing decisions along edges to higher ranks:
-// every graph vertex counts the occurrences of lower-ranked graph neighbours in its
-// live clauses; a vertex with none is in. A vertex that goes in sends every higher
-// neighbour out; a vertex that goes out decrements its higher neighbours' counts, and
-// a count reaching zero means every lower neighbour is out, so that vertex goes in.
-// Each wave processes only the vertices decided in the previous one. A neighbour
-// shared through several clauses is counted and decremented once per clause.
-// Vertices with more than MIS_WARP_MIN_OCC clauses are handled by a whole warp.
+// The independent set is decided in rounds of two phases:
+//   push: every vertex that went in during the last round marks its undecided
+//         higher-ranked neighbours out;
+//   pull: every undecided vertex walks its live clauses, from where its last walk
+//         stopped, looking at its lower-ranked graph neighbours; the first one
+//         that is not out stops the walk (the vertex stays undecided and resumes
+//         there), and a walk that reaches the end finds every lower neighbour out,
+//         so the vertex goes in.
+// A vertex goes in exactly when all its lower neighbours are out, and out when a
+// lower neighbour is in, as in the greedy walk in rank order. Out is final, so the
+// clauses a walk has passed never need another look. Vertices with more than
+// MIS_WARP_MIN_OCC clauses are walked by a whole warp.
 constexpr u32 MIS_WARP_MIN_OCC = 32;
 
 struct MisFront {
-    u32* small;   // next frontier, small adjacency
+    u32* small;   // list of small-adjacency vertices
     u32* nsmall;
-    u32* big;     // next frontier, large adjacency
+    u32* big;     // list of large-adjacency vertices
     u32* nbig;
 };
 
@@ -100,15 +104,13 @@ HD void mis_append(const MisFront& f, const Ctx& c, u32 v, bool pred) {
     if (big) f.big[pb] = v;
 }
 
-// Graph membership, and the list of large graph vertices for the warp count.
-HD void k_mis_init(const LcveArgs& a, const MisFront& bigs, u32 v) {
+// Graph membership; every graph vertex starts on the undecided lists.
+HD void k_mis_init(const LcveArgs& a, const MisFront& und, u32 v) {
     const u32 f = v ? fid_of(a.c, v) : 0u;
     const bool in_graph = v && (!a.f_active || a.f_active[f]) && lcve_valid(a.c, v) && lcve_freezable(a, v) &&
                           a.rank[v] < a.bound[2 * f];
     a.word[v] = in_graph ? a.rank[v] : NONE;
-    const bool big = in_graph && mis_is_big(a.c, v);
-    const u32 pb = warp_append(bigs.nbig, big);
-    if (big) bigs.big[pb] = v;
+    mis_append(und, a.c, v, in_graph);
 }
 
 // The clause walks read literals four at a time, so the loads (and the pushes'
@@ -120,16 +122,6 @@ constexpr u32 MIS_CHUNK = 4;
 // literals and its size and deleted bit (built once per election by k_mis_rec), so
 // clauses of up to three literals cost one load; longer ones read the rest of
 // their literals from the store.
-HD void k_mis_rec(const Ctx& c, Q4* rec, u32 i) {
-    const Hdr h = c.hdr[i];
-    const u32* l = c.lits + h.start;
-    Q4 q;
-    q.x = h.size > 0 ? l[0] : 0u;
-    q.y = h.size > 1 ? l[1] : 0u;
-    q.z = h.size > 2 ? l[2] : 0u;
-    q.w = h.size | (h_deleted(h.flags) ? 0x80000000u : 0u);
-    rec[i] = q;
-}
 struct MisCl {
     Q4 q;
     u32 r;
@@ -150,243 +142,150 @@ HD const u32* mis_long_lits(const LcveArgs& a, const MisCl& cl) {
     return cl.size() > 3 ? a.c.lits + hdr_ro(&a.c.hdr[cl.r]).start : nullptr;
 }
 
-// Occurrences of graph vertices ranked below rv (other than v) in clause r, and
-// the clause's bytes (8 + 4*len when live) added to ws.
-HD u32 mis_lower_in_hdr(const LcveArgs& a, u32 v, u32 rv, const MisCl& cl, u64& ws) {
-    if (cl.deleted()) return 0;
+// The record of clause i, and the graph's working set: every graph vertex's list
+// entry (4 bytes) and, for a live clause, its header and literals (8 + 4*len) once
+// per graph vertex in it. Runs after k_mis_init.
+HD void k_mis_rec(const LcveArgs& a, Q4* rec, u32 i) {
+    const Ctx& c = a.c;
+    const Hdr h = c.hdr[i];
+    const u32* l = c.lits + h.start;
+    Q4 q;
+    q.x = h.size > 0 ? l[0] : 0u;
+    q.y = h.size > 1 ? l[1] : 0u;
+    q.z = h.size > 2 ? l[2] : 0u;
+    q.w = h.size | (h_deleted(h.flags) ? 0x80000000u : 0u);
+    rec[i] = q;
+    u32 ng = 0;
+    for (u32 k = 0; k < h.size; k++) ng += mis_rank(a.word[ABS(l[k])]) != NONE ? 1u : 0u;
+    warp_sum_add64(a.ws_bytes, (u64)ng * (4ull + (h_deleted(h.flags) ? 0ull : 8ull + 4ull * h.size)));
+}
+
+// Whether clause cl holds a graph neighbour of v ranked below rv that is not out
+// (decisions are read through to the cache level other SMs write).
+HD bool mis_blocked_in(const LcveArgs& a, u32 v, u32 rv, const MisCl& cl) {
+    if (cl.deleted()) return false;
     const u32 size = cl.size();
-    ws += 8ull + 4ull * size;
     const u32* L = mis_long_lits(a, cl);
-    u32 n = 0;
     for (u32 k0 = 0; k0 < size; k0 += MIS_CHUNK) {
         u32 w[MIS_CHUNK];
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < size ? ABS(mis_lit(cl, L, k0 + j)) : v;
+        bool b = false;
 #pragma unroll
-        for (u32 j = 0; j < MIS_CHUNK; j++) n += (w[j] != v && mis_rank(a.word[w[j]]) < rv) ? 1u : 0u;
+        for (u32 j = 0; j < MIS_CHUNK; j++) {
+            if (w[j] == v) continue;
+            const u64 g = vload64(&a.word[w[j]]);
+            b |= mis_rank(g) < rv && mis_dec(g) != MIS_OUT;
+        }
+        if (b) return true;
     }
-    return n;
-}
-HD u32 mis_lower_in_clause(const LcveArgs& a, u32 v, u32 rv, u32 r, u64& ws) {
-    return mis_lower_in_hdr(a, v, rv, mis_cl(a, r), ws);
+    return false;
 }
 
-// Stores the lower-neighbour count of graph vertex v; a vertex with none goes in
-// and is returned true (the caller puts it on the first frontier).
-HD bool mis_set_count(const LcveArgs& a, u32 v, u32 rv, u32 n) {
-    if (n > MIS_CNT_MAX) {  // cannot be held: stop the election with an error
-        atom_or(a.c.err, ERR_CAP_SCRATCH);
-        n = MIS_CNT_MAX;
-    }
-    a.word[v] = (u64)rv | ((u64)n << 32) | (n ? 0ull : mis_dec_bits(MIS_IN));
-    return n == 0;
-}
-
-// The next clause's header is loaded before the current clause's literals are
-// examined, so two clause walks overlap.
-HD bool mis_count_one(const LcveArgs& a, u32 v, u64& ws) {
-    const u32 rv = mis_rank(a.word[v]);
-    const u32 p = V2L(v), np = a.c.ot_size[p], n_all = np + a.c.ot_size[p + 1];
+// Pull walk of undecided vertex v by one thread: true when v went in; otherwise the
+// resume point is stored (v stays undecided). The next clause's record is loaded
+// before the current one is examined.
+HD bool mis_pull_one(const LcveArgs& a, u32 v, u64 wv) {
+    const u32 rv = mis_rank(wv);
+    const u32 p = V2L(v), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
     const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
-    ws += 4ull * n_all;
-    u32 n = 0;
-    if (n_all) {
-        MisCl h = mis_cl(a, ldro(&a.c.ot_refs[op]));
-        for (u32 t = 0; t < n_all; t++) {
-            MisCl hn = h;
-            if (t + 1 < n_all) hn = mis_cl(a, ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1]));
-            n += mis_lower_in_hdr(a, v, rv, h, ws);
-            h = hn;
+    u32 t = mis_resume(wv);
+    if (t < n) {
+        MisCl cl = mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + t]));
+        for (; t < n; t++) {
+            MisCl nx = cl;
+            if (t + 1 < n) nx = mis_cl(a, ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1]));
+            if (mis_blocked_in(a, v, rv, cl)) {
+                a.word[v] = mis_with_resume(rv, t);
+                return false;
+            }
+            cl = nx;
         }
     }
-    return mis_set_count(a, v, rv, n);
+    atom_or64(&a.word[v], mis_dec_bits(MIS_IN));
+    return true;
 }
 
-// Count for the small graph vertices (the large ones go through the warp kernel).
-HD void k_mis_count(const LcveArgs& a, const MisFront& f, u32 v) {
-    u64 ws = 0;
-    const bool in0 = v && mis_rank(a.word[v]) != NONE && !mis_is_big(a.c, v) && mis_count_one(a, v, ws);
-    mis_append(f, a.c, v, in0);
-    warp_sum_add64(a.ws_bytes, ws);
-}
-
-// Frontier vertex u (rank ru, in or out) pushes its decision to its higher
-// neighbours in clause r; app(w) is called for each neighbour w this decides. An
-// in vertex marks them out; an out vertex decrements their counts unconditionally
-// (a decided neighbour's count no longer matters; a count cannot fall below the
-// occurrences of a lower neighbour that is in, which never decrements), and the
-// push that takes a count from one to zero marks that neighbour in: no other push
-// can reach it any more.
-template <class App>
-HD void mis_push_clause(const LcveArgs& a, u32 u, u32 ru, bool in, const MisCl& cl, App app) {
+// Push of in vertex u (rank ru) through clause cl: undecided higher neighbours go
+// out. The rank in a neighbour's word never changes and a decision is final, so a
+// plain (possibly older) load decides whether the atomic is needed.
+HD void mis_push_clause(const LcveArgs& a, u32 u, u32 ru, const MisCl& cl) {
     if (cl.deleted()) return;
     const u32 size = cl.size();
     const u32* L = mis_long_lits(a, cl);
     for (u32 k0 = 0; k0 < size; k0 += MIS_CHUNK) {
         u32 w[MIS_CHUNK];
-        u64 old[MIS_CHUNK];
-        bool up[MIS_CHUNK];
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) w[j] = k0 + j < size ? ABS(mis_lit(cl, L, k0 + j)) : u;
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) {
-            const u32 g = w[j] != u ? mis_rank(a.word[w[j]]) : NONE;
-            up[j] = g != NONE && g > ru;
-        }
-#pragma unroll
-        for (u32 j = 0; j < MIS_CHUNK; j++)
-            if (up[j]) old[j] = in ? atom_or64(&a.word[w[j]], mis_dec_bits(MIS_OUT)) : atom_add64(&a.word[w[j]], 0ull - MIS_CNT_ONE);
-#pragma unroll
-        for (u32 j = 0; j < MIS_CHUNK; j++) {
-            if (!up[j] || mis_dec(old[j]) != MIS_UNDECIDED) continue;
-            if (in) {
-                app(w[j]);
-            } else if (mis_cnt(old[j]) == 1u) {
-                atom_or64(&a.word[w[j]], mis_dec_bits(MIS_IN));
-                app(w[j]);
-            }
+            if (w[j] == u) continue;
+            const u64 g = a.word[w[j]];
+            if (mis_rank(g) != NONE && mis_rank(g) > ru && mis_dec(g) == MIS_UNDECIDED)
+                atom_or64(&a.word[w[j]], mis_dec_bits(MIS_OUT));
         }
     }
 }
 
-// Frontier vertex u pushes through all its clauses. The next clause's header is
-// loaded before the current clause's atomics, so two clause walks overlap.
-template <class App>
-HD void mis_push_vertex(const LcveArgs& a, u32 u, App app) {
-    const u64 wu = vload64(&a.word[u]);
-    const bool in = mis_dec(wu) == MIS_IN;
-    const u32 ru = mis_rank(wu);
+HD void mis_push_vertex(const LcveArgs& a, u32 u) {
+    const u32 ru = mis_rank(a.word[u]);
     const u32 p = V2L(u), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
     const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
     if (!n) return;
-    MisCl h = mis_cl(a, ldro(&a.c.ot_refs[op]));
+    MisCl cl = mis_cl(a, ldro(&a.c.ot_refs[op]));
     for (u32 t = 0; t < n; t++) {
-        MisCl hn = h;
-        if (t + 1 < n) hn = mis_cl(a, ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1]));
-        mis_push_clause(a, u, ru, in, h, app);
-        h = hn;
+        MisCl nx = cl;
+        if (t + 1 < n) nx = mis_cl(a, ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1]));
+        mis_push_clause(a, u, ru, cl);
+        cl = nx;
     }
 }
 
 #if !SIGMA_CUDA
-HD void k_mis_count_big(const LcveArgs& a, const u32* in, const MisFront& f, u32 idx) {
+// Serial rounds of the emulation build: the same phases over the same lists.
+HD void k_mis_push(const LcveArgs& a, const u32* in, u32 idx) { mis_push_vertex(a, in[idx]); }
+HD void k_mis_pull(const LcveArgs& a, const u32* in, const MisFront& und, const MisFront& ins, u32 idx) {
     const u32 v = in[idx];
-    u64 ws = 0;
-    if (mis_count_one(a, v, ws)) f.big[atom_add(f.nbig, 1u)] = v;
-    *a.ws_bytes += ws;
-}
-// One wave step of the serial build: frontier vertex in[idx] pushes, decided
-// vertices go straight to the next lists.
-HD void k_mis_push(const LcveArgs& a, const u32* in, const MisFront& f, u32 idx) {
-    mis_push_vertex(a, in[idx], [&](u32 w) {
-        if (mis_is_big(a.c, w)) f.big[atom_add(f.nbig, 1u)] = w;
-        else f.small[atom_add(f.nsmall, 1u)] = w;
-    });
+    const u64 wv = a.word[v];
+    if (mis_dec(wv) != MIS_UNDECIDED) return;
+    const bool big = mis_is_big(a.c, v);
+    if (mis_pull_one(a, v, wv)) {
+        if (big) ins.big[atom_add(ins.nbig, 1u)] = v;
+        else ins.small[atom_add(ins.nsmall, 1u)] = v;
+    } else {
+        if (big) und.big[atom_add(und.nbig, 1u)] = v;
+        else und.small[atom_add(und.nsmall, 1u)] = v;
+    }
 }
 #else
-// Count for the small graph vertices with a warp per 32 consecutive variables: the
-// clauses of the 32 are spread over the lanes (as in the waves), each lane adds its
-// clauses' lower-neighbour occurrences to the owner's counter in shared memory.
-__global__ void __launch_bounds__(256) mis_count_flat_k(LcveArgs a, MisFront f, u32 nvars) {
-    __shared__ u32 acc[8][32];
-    const u32 lane = threadIdx.x & 31u, wl = threadIdx.x >> 5;
-    const u32 nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (u32 base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; base <= nvars; base += nwarps * 32u) {
-        const u32 v = base + lane;
-        const u64 wv = (v && v <= nvars) ? a.word[v] : (u64)NONE;
-        const bool counted = mis_rank(wv) != NONE && !mis_is_big(a.c, v);
-        const u32 p = V2L(v);
-        const u32 np = counted ? a.c.ot_size[p] : 0u, cnt = counted ? np + a.c.ot_size[p + 1] : 0u;
-        const u32 op = counted ? a.c.ot_off[p] : 0u, on = counted ? a.c.ot_off[p + 1] : 0u;
-        u64 ws = 4ull * cnt;
-        acc[wl][lane] = 0;
-        u32 incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const u32 t = __shfl_up_sync(0xffffffffu, incl, o);
-            if ((int)lane >= o) incl += t;
-        }
-        const u32 start = incl - cnt;
-        const u32 total = __shfl_sync(0xffffffffu, incl, 31);
-        __syncwarp();
-        for (u32 t0 = 0; t0 < total; t0 += 32u) {
-            const u32 t = t0 + lane;
-            u32 lo = 0;
-#pragma unroll
-            for (u32 step = 16; step; step >>= 1) {
-                const u32 s_mid = __shfl_sync(0xffffffffu, start, (int)(lo + step));
-                if (lo + step < 32u && s_mid <= t) lo += step;
-            }
-            const u32 ov = __shfl_sync(0xffffffffu, v, (int)lo);
-            const u64 owv = __shfl_sync(0xffffffffu, wv, (int)lo);
-            const u32 onp = __shfl_sync(0xffffffffu, np, (int)lo);
-            const u32 oop = __shfl_sync(0xffffffffu, op, (int)lo);
-            const u32 oon = __shfl_sync(0xffffffffu, on, (int)lo);
-            const u32 ost = __shfl_sync(0xffffffffu, start, (int)lo);
-            if (t < total) {
-                const u32 k = t - ost;
-                const u32 r = ldro(&a.c.ot_refs[k < onp ? oop + k : oon + (k - onp)]);
-                const u32 nl = mis_lower_in_hdr(a, ov, mis_rank(owv), mis_cl(a, r), ws);
-                if (nl) atomicAdd(&acc[wl][lo], nl);
-            }
-        }
-        __syncwarp();
-        const bool in0 = counted && mis_set_count(a, v, mis_rank(wv), acc[wl][lane]);
-        mis_append(f, a.c, v, in0);
-        warp_sum_add64(a.ws_bytes, ws);
-        __syncwarp();
-    }
-}
-
-// Count for the large graph vertices, one warp each (lanes take its clauses). The
-// list length is read from device memory (no host round trip).
-__global__ void mis_count_warp_k(LcveArgs a, const u32* in, const u32* n_ptr, MisFront f) {
-    const u32 lane = threadIdx.x & 31u, nw = (gridDim.x * blockDim.x) >> 5;
-    const u32 n = *n_ptr;
-    for (u32 idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < n; idx += nw) {
-        const u32 v = in[idx];
-        const u32 rv = mis_rank(a.word[v]);
-        const u32 p = V2L(v), np = a.c.ot_size[p], nn = a.c.ot_size[p + 1];
-        const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
-        u32 cnt = 0;
-        u64 ws = 0;
-        for (u32 t = lane; t < np + nn; t += 32)
-            cnt += mis_lower_in_clause(a, v, rv, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)]), ws);
-        cnt = __reduce_add_sync(0xffffffffu, cnt);
-        for (int o = 16; o; o >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, o);
-        if (lane == 0) {
-            atomicAdd((unsigned long long*)a.ws_bytes, (unsigned long long)(ws + 4ull * (np + nn)));
-            if (mis_set_count(a, v, rv, cnt)) f.big[atomicAdd(f.nbig, 1u)] = v;
-        }
-        __syncwarp();
-    }
-}
-
-// All frontier waves in one cooperative launch. Wave k reads the lists small[k&1],
-// big[k&1] with lengths in counter pair k%3 and appends to the other lists through
-// pair (k+1)%3; pair (k+2)%3, last read in wave k-1, is cleared for wave k+1. A
-// grid barrier separates the waves.
-struct MisWaves {
-    u32* small[2];
-    u32* big[2];
-    u32* ctr;        // three (small, big) length pairs; pair 0 holds the first frontier
+// All rounds in one cooperative launch. Round r reads the undecided and new-in
+// lists u[r&1], in[r&1] (lengths in counter set r%3: undecided small, large, in
+// small, large) and writes u[(r+1)&1], in[(r+1)&1] through counter set (r+1)%3;
+// set (r+2)%3, last read in round r-1, is cleared for round r+1. Grid barriers
+// separate the push phase, the pull phase and the rounds.
+struct MisRounds {
+    u32* u_small[2];
+    u32* u_big[2];
+    u32* in_small[2];
+    u32* in_big[2];
+    u32* ctr;        // three sets of four counters
     u32* bar;        // grid barrier: [0] arrivals, [1] generation
-    u32* waves;      // out: number of waves run
-    u32 max_waves;
+    u32* rounds;     // out: rounds run
+    u32 max_rounds;
 };
 
-// Vertices decided in a wave are staged per block in shared memory and copied to
-// the next lists with one reservation per block (a vertex that finds its block's
-// queue full goes to the list directly).
-constexpr u32 MIS_QCAP = 2048;
+// Vertices leaving a pull phase are staged per block in shared memory and copied
+// to the next lists with one reservation per block (a vertex that finds its
+// block's queue full goes to the list directly).
+constexpr u32 MIS_QCAP = 1024;
 
 struct MisBlockQueue {
     u32 small[MIS_QCAP], big[MIS_QCAP];
     u32 ns, nb, base_s, base_b;
 };
 
-DEV void mis_queue_push(MisBlockQueue& q, const MisFront& f, const Ctx& c, u32 w) {
-    if (mis_is_big(c, w)) {
+DEV void mis_queue_push(MisBlockQueue& q, const MisFront& f, bool big, u32 w) {
+    if (big) {
         const u32 k = atomicAdd(&q.nb, 1u);
         if (k < MIS_QCAP) q.big[k] = w;
         else f.big[atomicAdd(f.nbig, 1u)] = w;
@@ -411,89 +310,86 @@ DEV void mis_queue_flush(MisBlockQueue& q, const MisFront& f) {
     if (threadIdx.x == 0) q.ns = q.nb = 0;
 }
 
-__global__ void __launch_bounds__(256) mis_waves_k(LcveArgs a, MisWaves w) {
-    __shared__ MisBlockQueue q;
+__global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
+    __shared__ MisBlockQueue qu, qi;
     const u32 tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const u32 lane = threadIdx.x & 31u, nwarps = nth >> 5;
-    if (threadIdx.x == 0) q.ns = q.nb = 0;
+    if (threadIdx.x == 0) qu.ns = qu.nb = qi.ns = qi.nb = 0;
     __syncthreads();
-    for (u32 wave = 0;; wave++) {
-        const u32 cur = wave % 3, nxt = (wave + 1) % 3, old = (wave + 2) % 3;
-        const u32 ns = vload(&w.ctr[2 * cur]), nb = vload(&w.ctr[2 * cur + 1]);
-        if (!ns && !nb) {
-            if (tid == 0) *w.waves = wave;
+    for (u32 r = 0;; r++) {
+        const u32 cur = r % 3, nxt = (r + 1) % 3, old = (r + 2) % 3;
+        const u32 us = vload(&w.ctr[4 * cur]), ub = vload(&w.ctr[4 * cur + 1]);
+        const u32 is = vload(&w.ctr[4 * cur + 2]), ib = vload(&w.ctr[4 * cur + 3]);
+        if (!us && !ub && !is && !ib) {
+            if (tid == 0) *w.rounds = r;
             return;
         }
-        if (wave >= w.max_waves) {
+        if (r >= w.max_rounds) {
             if (tid == 0) atomicOr(a.c.err, ERR_ITER);
             return;
         }
-        if (tid == 0) {
-            w.ctr[2 * old] = 0;
-            w.ctr[2 * old + 1] = 0;
-        }
-        MisFront f;
-        f.small = w.small[(wave + 1) & 1];
-        f.nsmall = &w.ctr[2 * nxt];
-        f.big = w.big[(wave + 1) & 1];
-        f.nbig = &w.ctr[2 * nxt + 1];
-        const auto app = [&](u32 v) { mis_queue_push(q, f, a.c, v); };
-        // the lists were written in the previous wave by other blocks: read them uncached
-        const u32* in_b = w.big[wave & 1];
-        for (u32 idx = tid >> 5; idx < nb; idx += nwarps) {
-            const u32 u = vload(&in_b[idx]);
-            const u64 wu = vload64(&a.word[u]);
-            const bool uin = mis_dec(wu) == MIS_IN;
-            const u32 ru = mis_rank(wu);
+        if (tid == 0)
+            for (u32 k = 0; k < 4; k++) w.ctr[4 * old + k] = 0;
+        // push: the vertices that went in last round (lists written by other blocks: uncached reads)
+        const u32* pin_b = w.in_big[r & 1];
+        for (u32 idx = tid >> 5; idx < ib; idx += nwarps) {
+            const u32 u = vload(&pin_b[idx]);
+            const u32 ru = mis_rank(a.word[u]);
             const u32 p = V2L(u), np = a.c.ot_size[p], nn = a.c.ot_size[p + 1];
             const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
             for (u32 t = lane; t < np + nn; t += 32)
-                mis_push_clause(a, u, ru, uin, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])), app);
+                mis_push_clause(a, u, ru, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])));
             __syncwarp();
         }
-        // small vertices: a warp takes 32 of them and spreads all their clauses over
-        // its lanes (a prefix of the clause counts maps each lane's clause to its
-        // vertex), so every lane walks about as many clauses as the others
-        const u32* in_s = w.small[wave & 1];
-        for (u32 base = (tid >> 5) * 32u; base < ns; base += nwarps * 32u) {
-            const u32 idx = base + lane;
-            const u32 u = idx < ns ? vload(&in_s[idx]) : 0u;
-            const u64 wu = u ? vload64(&a.word[u]) : 0ull;
-            const u32 p = V2L(u);
-            const u32 np = u ? a.c.ot_size[p] : 0u, cnt = u ? np + a.c.ot_size[p + 1] : 0u;
-            const u32 op = u ? a.c.ot_off[p] : 0u, on = u ? a.c.ot_off[p + 1] : 0u;
-            u32 incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const u32 t = __shfl_up_sync(0xffffffffu, incl, o);
-                if ((int)lane >= o) incl += t;
+        const u32* pin_s = w.in_small[r & 1];
+        for (u32 idx = tid; idx < is; idx += nth) mis_push_vertex(a, vload(&pin_s[idx]));
+        if (!grid_barrier(w.bar, a.c.err)) return;
+        // pull: the undecided vertices
+        MisFront fu, fi;
+        fu.small = w.u_small[(r + 1) & 1];
+        fu.nsmall = &w.ctr[4 * nxt];
+        fu.big = w.u_big[(r + 1) & 1];
+        fu.nbig = &w.ctr[4 * nxt + 1];
+        fi.small = w.in_small[(r + 1) & 1];
+        fi.nsmall = &w.ctr[4 * nxt + 2];
+        fi.big = w.in_big[(r + 1) & 1];
+        fi.nbig = &w.ctr[4 * nxt + 3];
+        const u32* pu_b = w.u_big[r & 1];
+        for (u32 idx = tid >> 5; idx < ub; idx += nwarps) {
+            const u32 v = vload(&pu_b[idx]);
+            const u64 wv = vload64(&a.word[v]);
+            if (mis_dec(wv) != MIS_UNDECIDED) continue;  // warp-uniform
+            const u32 rv = mis_rank(wv);
+            const u32 p = V2L(v), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
+            const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
+            u32 stop = NONE;
+            for (u32 b0 = mis_resume(wv); b0 < n && stop == NONE; b0 += 32) {
+                const u32 t = b0 + lane;
+                const bool blk = t < n && mis_blocked_in(a, v, rv, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])));
+                const u32 m = __ballot_sync(0xffffffffu, blk);
+                if (m) stop = b0 + (u32)(__ffs(m) - 1);
             }
-            const u32 start = incl - cnt;
-            const u32 total = __shfl_sync(0xffffffffu, incl, 31);
-            for (u32 t0 = 0; t0 < total; t0 += 32u) {
-                const u32 t = t0 + lane;
-                // owner: the last lane whose start is <= t
-                u32 lo = 0;
-#pragma unroll
-                for (u32 step = 16; step; step >>= 1) {
-                    const u32 s_mid = __shfl_sync(0xffffffffu, start, (int)(lo + step));
-                    if (lo + step < 32u && s_mid <= t) lo += step;
+            if (lane == 0) {
+                if (stop != NONE) {
+                    a.word[v] = mis_with_resume(rv, stop);
+                    mis_queue_push(qu, fu, true, v);
+                } else {
+                    atomicOr((unsigned long long*)&a.word[v], (unsigned long long)mis_dec_bits(MIS_IN));
+                    mis_queue_push(qi, fi, true, v);
                 }
-                const u32 ou = __shfl_sync(0xffffffffu, u, (int)lo);
-                const u64 owu = __shfl_sync(0xffffffffu, wu, (int)lo);
-                const u32 onp = __shfl_sync(0xffffffffu, np, (int)lo);
-                const u32 oop = __shfl_sync(0xffffffffu, op, (int)lo);
-                const u32 oon = __shfl_sync(0xffffffffu, on, (int)lo);
-                const u32 ost = __shfl_sync(0xffffffffu, start, (int)lo);
-                if (t < total) {
-                    const u32 k = t - ost;
-                    const u32 r = ldro(&a.c.ot_refs[k < onp ? oop + k : oon + (k - onp)]);
-                    mis_push_clause(a, ou, mis_rank(owu), mis_dec(owu) == MIS_IN, mis_cl(a, r), app);
-                }
-                __syncwarp();
             }
+            __syncwarp();
         }
-        mis_queue_flush(q, f);
+        const u32* pu_s = w.u_small[r & 1];
+        for (u32 idx = tid; idx < us; idx += nth) {
+            const u32 v = vload(&pu_s[idx]);
+            const u64 wv = vload64(&a.word[v]);
+            if (mis_dec(wv) != MIS_UNDECIDED) continue;
+            if (mis_pull_one(a, v, wv)) mis_queue_push(qi, fi, false, v);
+            else mis_queue_push(qu, fu, false, v);
+        }
+        mis_queue_flush(qu, fu);
+        mis_queue_flush(qi, fi);
         if (!grid_barrier(w.bar, a.c.err)) return;
     }
 }

@@ -45,15 +45,15 @@ struct FPropClause { PropArgs a; HD void operator()(u32 i) const { k_prop_clause
 struct FReduce { Ctx c; HD void operator()(u32 i) const { k_reduce_list(c, i); } };
 struct FScores { LcveArgs a; u32* max_score; HD void operator()(u32 i) const { k_scores(a, max_score, i); } };
 struct FRank { LcveArgs a; HD void operator()(u32 i) const { k_rank(a, i); } };
-struct FMisRec { Ctx c; Q4* rec; HD void operator()(u32 i) const { k_mis_rec(c, rec, i); } };
+struct FMisRec { LcveArgs a; Q4* rec; HD void operator()(u32 i) const { k_mis_rec(a, rec, i); } };
+#if !SIGMA_CUDA
+struct FMisPush { LcveArgs a; const u32* in; HD void operator()(u32 i) const { k_mis_push(a, in, i); } };
+struct FMisPull {
+    LcveArgs a; const u32* in; MisFront und, ins;
+    HD void operator()(u32 i) const { k_mis_pull(a, in, und, ins, i); }
+};
+#endif
 struct FMisInit { LcveArgs a; MisFront b; HD void operator()(u32 i) const { k_mis_init(a, b, i); } };
-#if !SIGMA_CUDA
-struct FMisCount { LcveArgs a; MisFront f; HD void operator()(u32 i) const { k_mis_count(a, f, i); } };
-#endif
-#if !SIGMA_CUDA
-struct FMisPush { LcveArgs a; const u32* in; MisFront f; HD void operator()(u32 i) const { k_mis_push(a, in, f, i); } };
-struct FMisCountBig { LcveArgs a; const u32* in; MisFront f; HD void operator()(u32 i) const { k_mis_count_big(a, in, f, i); } };
-#endif
 struct FMisBound { LcveArgs a; HD void operator()(u32 i) const { k_mis_bound(a, i); } };
 struct FElectFlag { LcveArgs a; u32* flags; HD void operator()(u32 i) const { k_elect_flag(a, flags, i); } };
 struct FElectWrite { LcveArgs a; const u32* flags; const u32* scan; HD void operator()(u32 i) const { k_elect_write(a, flags, scan, i); } };
@@ -258,6 +258,7 @@ struct pf_sigma_ctx {
     DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
     DBuf<u32> mis_big_a, mis_big_b;
     DBuf<u64> mis_word;
+    DBuf<u32> mis_in[4];  // new-in lists of the election rounds (small x2, large x2)
     DBuf<Q4> mis_rec;  // the election's 16-byte clause records
     DBuf<u32> pv_perm, pv_key;
     DBuf<u32> work, cl_stamp;
@@ -299,7 +300,7 @@ struct pf_sigma_ctx {
     pf_round_stats st;
     std::vector<uint32_t> dump;
     u64 alg_bytes = 0;
-    // hottest kernels, timed one by one: waves, BVE decision, SUB, BVE write
+    // hottest kernels, timed one by one: election rounds, BVE decision, SUB, BVE write
     enum { K_MIS, K_BVE, K_SUB, K_BVEW, K_COUNT };
     KernelClock kclock[K_COUNT];
     u64 kbytes[K_COUNT] = {};
@@ -367,7 +368,7 @@ struct pf_sigma_ctx {
         }
         return cache;
     }
-    int mis_waves_grid() { return coop_grid(mis_waves_k, mis_grid); }
+    int mis_rounds_grid() { return coop_grid(mis_rounds_k, mis_grid); }
 #endif
     void write_u64(u64* d, u64 v) { rt.h2d(d, &v, 8); }
 
@@ -631,55 +632,53 @@ struct pf_sigma_ctx {
         rt.launches += 5 * (bits / 8);
         rt.zero(bound.p, (size_t)nform * 8, 0xFF);
         rt.each(FRank{a}, nvars);
-        // Independent set by frontier waves. The frontier lists (small / large
-        // adjacency) alternate between flags|mis_big_a and flags_scan|mis_big_b.
+        // Independent set by push/pull rounds. Undecided lists: flags|mis_big_a and
+        // flags_scan|mis_big_b; new-in lists: mis_in[0..3].
         mis_big_a.reserve(rt, nvars + 1);
         mis_big_b.reserve(rt, nvars + 1);
-        u32* ctr = counters.p + 12;  // [12..17] frontier lengths, [18..19] barrier, [20] waves
-        rt.zero(ctr, 9 * 4);
-        rt.each(FMisInit{a, MisFront{nullptr, nullptr, mis_big_b.p, ctr + 3}}, nvars + 1);
-        rt.each(FMisRec{a.c, mis_rec.p}, ncls);
-        MisFront f0{flags.p, ctr, mis_big_a.p, ctr + 1};
+        for (auto& b : mis_in) b.reserve(rt, nvars + 1);
+        u32* ctr = counters.p + 12;  // [12..23] three sets of list lengths, [24..25] barrier, [26] rounds
+        rt.zero(ctr, 15 * 4);
+        rt.each(FMisInit{a, MisFront{flags.p, ctr, mis_big_a.p, ctr + 1}}, nvars + 1);
+        rt.each(FMisRec{a, mis_rec.p}, ncls);
         u32 rounds = 0;
 #if SIGMA_CUDA
-        rt.launches += 3;
-        mis_count_flat_k<<<rt.grid(nvars + 1, 8), 256, 0, rt.stream>>>(a, f0, nvars);
-        ck(cudaGetLastError(), "launch");
-        mis_count_warp_k<<<rt.sms * 8, 256, 0, rt.stream>>>(a, mis_big_b.p, ctr + 3, f0);
-        ck(cudaGetLastError(), "launch");
-        MisWaves w;
-        w.small[0] = flags.p;
-        w.small[1] = flags_scan.p;
-        w.big[0] = mis_big_a.p;
-        w.big[1] = mis_big_b.p;
+        MisRounds w;
+        w.u_small[0] = flags.p;
+        w.u_small[1] = flags_scan.p;
+        w.u_big[0] = mis_big_a.p;
+        w.u_big[1] = mis_big_b.p;
+        w.in_small[0] = mis_in[0].p;
+        w.in_small[1] = mis_in[1].p;
+        w.in_big[0] = mis_in[2].p;
+        w.in_big[1] = mis_in[3].p;
         w.ctr = ctr;
-        w.bar = ctr + 6;
-        w.waves = ctr + 8;
-        w.max_waves = nvars + 2;
-        rt.zero(ctr + 2, 4 * 4);  // the count-list length in pair 1, and the barrier
+        w.bar = ctr + 12;
+        w.rounds = ctr + 14;
+        w.max_rounds = nvars + 2;
         void* args[] = {&a, &w};
         kclock[K_MIS].start(rt);
-        ck(cudaLaunchCooperativeKernel((const void*)mis_waves_k, dim3(mis_waves_grid()), dim3(256), args, 0, rt.stream),
+        ck(cudaLaunchCooperativeKernel((const void*)mis_rounds_k, dim3(mis_rounds_grid()), dim3(256), args, 0,
+                                       rt.stream),
            "cooperative launch");
         kclock[K_MIS].stop(rt);
         rt.launches++;
         check();
-        rounds = read_u32(ctr + 8);
+        rounds = read_u32(ctr + 14);
 #else
-        rt.each(FMisCount{a, f0}, nvars + 1);
-        rt.each(FMisCountBig{a, mis_big_b.p, f0}, read_u32(ctr + 3));
-        MisFront fin = f0;
-        MisFront fout{flags_scan.p, ctr + 2, mis_big_b.p, ctr + 3};
-        u32 pend[2];
-        rt.d2h(pend, ctr, 8);
+        MisFront und[2] = {{flags.p, ctr, mis_big_a.p, ctr + 1}, {flags_scan.p, ctr + 4, mis_big_b.p, ctr + 5}};
+        MisFront ins[2] = {{mis_in[0].p, ctr + 2, mis_in[2].p, ctr + 3}, {mis_in[1].p, ctr + 6, mis_in[3].p, ctr + 7}};
         kclock[K_MIS].start(rt);
-        while (pend[0] || pend[1]) {
+        for (u32 cur = 0;; cur ^= 1u) {
+            u32 n[4];
+            rt.d2h(n, ctr + 4 * cur, 16);
+            if (!n[0] && !n[1] && !n[2] && !n[3]) break;
             if (++rounds > nvars + 2) throw int(PF_ETIMEOUT);
-            rt.zero(fout.nsmall, 8);
-            if (pend[0]) rt.each(FMisPush{a, fin.small, fout}, pend[0]);
-            if (pend[1]) rt.each(FMisPush{a, fin.big, fout}, pend[1]);
-            std::swap(fin, fout);
-            rt.d2h(pend, fin.nsmall, 8);
+            if (n[2]) rt.each(FMisPush{a, ins[cur].small}, n[2]);
+            if (n[3]) rt.each(FMisPush{a, ins[cur].big}, n[3]);
+            rt.zero(ctr + 4 * (cur ^ 1u), 16);
+            if (n[0]) rt.each(FMisPull{a, und[cur].small, und[cur ^ 1u], ins[cur ^ 1u]}, n[0]);
+            if (n[1]) rt.each(FMisPull{a, und[cur].big, und[cur ^ 1u], ins[cur ^ 1u]}, n[1]);
         }
         kclock[K_MIS].stop(rt);
 #endif
@@ -2089,6 +2088,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     for (auto* b : b64) b->free();
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
     c.mis_word.free();
+    for (auto& b : c.mis_in) b.free();
     c.mis_rec.free();
     c.res_mark.free();
 #if SIGMA_CUDA

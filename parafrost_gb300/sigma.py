@@ -35,7 +35,7 @@ class SigmaError(RuntimeError):
 
 
 # The kernels pf_round_stats times one by one (ms_kernel / bytes_kernel order).
-HOT_KERNELS = ("mis_waves", "bve_decide", "sub", "bve_write")
+HOT_KERNELS = ("mis_rounds", "bve_decide", "sub", "bve_write")
 
 
 class RoundStats(ctypes.Structure):
