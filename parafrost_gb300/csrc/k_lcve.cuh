@@ -84,7 +84,8 @@ HD void k_rank(const LcveArgs& a, u32 p) {
 // A vertex goes in exactly when all its lower neighbours are out, and out when a
 // lower neighbour is in, as in the greedy walk in rank order. Out is final, so the
 // clauses a walk has passed never need another look. Vertices with more than
-// MIS_WARP_MIN_OCC clauses are walked by a whole warp.
+// MIS_WARP_MIN_OCC clauses are walked by a whole warp; the others by one thread,
+// or by a group of lanes when few of them are left (mis_lanes).
 constexpr u32 MIS_WARP_MIN_OCC = 32;
 
 struct MisFront {
@@ -296,6 +297,36 @@ DEV void mis_queue_push(MisBlockQueue& q, const MisFront& f, bool big, u32 w) {
     }
 }
 
+// Append of the lanes with pred by one reservation per warp: to the block's queue
+// while it has room, the rest to the list. All lanes of the warp take part.
+DEV void mis_queue_warp(u32* qa, u32& qn, u32* list, u32* nlist, bool pred, u32 v) {
+    const u32 lane = threadIdx.x & 31u;
+    const u32 m = __ballot_sync(kFull, pred);
+    if (!m) return;
+    const u32 cnt = (u32)__popc(m), rank = (u32)__popc(m & ((1u << lane) - 1u));
+    u32 k = 0;
+    if (lane == 0) k = atomicAdd(&qn, cnt);
+    k = __shfl_sync(kFull, k, 0);
+    const u32 fit = k < MIS_QCAP ? (cnt < MIS_QCAP - k ? cnt : MIS_QCAP - k) : 0u;
+    u32 g = 0;
+    if (lane == 0 && cnt > fit) g = atomicAdd(nlist, cnt - fit);
+    g = __shfl_sync(kFull, g, 0);
+    if (pred) {
+        if (rank < fit) qa[k + rank] = v;
+        else list[g + rank - fit] = v;
+    }
+}
+
+// Lanes per vertex for a phase over n small vertices and nth threads: when the list
+// is short, each vertex's clauses are spread over a group of up to 32 lanes, so the
+// phase waits for one clause walk per vertex instead of a whole list walked by one
+// thread.
+DEV u32 mis_lanes(u32 n, u32 nth) {
+    u32 L = 1;
+    while (L < 32u && (u64)n * (2u * L) <= nth) L *= 2u;
+    return L;
+}
+
 DEV void mis_queue_flush(MisBlockQueue& q, const MisFront& f) {
     __syncthreads();
     const u32 ns = q.ns < MIS_QCAP ? q.ns : MIS_QCAP, nb = q.nb < MIS_QCAP ? q.nb : MIS_QCAP;
@@ -342,7 +373,21 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
             __syncwarp();
         }
         const u32* pin_s = w.in_small[r & 1];
-        for (u32 idx = tid; idx < is; idx += nth) mis_push_vertex(a, vload(&pin_s[idx]));
+        const u32 li = mis_lanes(is, nth);
+        if (li == 1) {
+            for (u32 idx = tid; idx < is; idx += nth) mis_push_vertex(a, vload(&pin_s[idx]));
+        } else {
+            // a group of li lanes per vertex, clauses strided over the group
+            const u32 sub = lane & (li - 1u);
+            for (u32 idx = tid / li; idx < is; idx += nth / li) {
+                const u32 u = vload(&pin_s[idx]);
+                const u32 ru = mis_rank(a.word[u]);
+                const u32 p = V2L(u), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
+                const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
+                for (u32 t = sub; t < n; t += li)
+                    mis_push_clause(a, u, ru, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + t])));
+            }
+        }
         if (!grid_barrier(w.bar, a.c.err)) return;
         // pull: the undecided vertices
         MisFront fu, fi;
@@ -381,12 +426,66 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
             __syncwarp();
         }
         const u32* pu_s = w.u_small[r & 1];
-        for (u32 idx = tid; idx < us; idx += nth) {
-            const u32 v = vload(&pu_s[idx]);
-            const u64 wv = vload64(&a.word[v]);
-            if (mis_dec(wv) != MIS_UNDECIDED) continue;
-            if (mis_pull_one(a, v, wv)) mis_queue_push(qi, fi, false, v);
-            else mis_queue_push(qu, fu, false, v);
+        const u32 lu = mis_lanes(us, nth);
+        if (lu == 1) {
+            // warp-uniform trip count: the appends below take every lane
+            for (u32 base = tid - lane; base < us; base += nth) {
+                const u32 idx = base + lane;
+                u32 v = 0;
+                bool in = false, und = false;
+                if (idx < us) {
+                    v = vload(&pu_s[idx]);
+                    const u64 wv = vload64(&a.word[v]);
+                    if (mis_dec(wv) == MIS_UNDECIDED) {
+                        in = mis_pull_one(a, v, wv);
+                        und = !in;
+                    }
+                }
+                mis_queue_warp(qi.small, qi.ns, fi.small, fi.nsmall, in, v);
+                mis_queue_warp(qu.small, qu.ns, fu.small, fu.nsmall, und, v);
+            }
+        } else {
+            // a group of lu lanes per vertex: batches of lu clauses in list order,
+            // the first blocking clause of a batch (lowest lane) stops the walk
+            const u32 sub = lane & (lu - 1u), gbase = lane - sub;
+            const u32 gmask = lu == 32u ? kFull : ((1u << lu) - 1u) << gbase;
+            const u32 gpw = 32u / lu;
+            for (u32 base = (tid >> 5) * gpw; base < us; base += nwarps * gpw) {
+                const u32 idx = base + lane / lu;
+                u32 v = 0;
+                bool in = false, und = false;
+                if (idx < us) {
+                    v = vload(&pu_s[idx]);
+                    const u64 wv = vload64(&a.word[v]);
+                    if (mis_dec(wv) == MIS_UNDECIDED) {  // the same word for the whole group
+                        const u32 rv = mis_rank(wv);
+                        const u32 p = V2L(v), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
+                        const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
+                        u32 stop = NONE;
+                        for (u32 b0 = mis_resume(wv); b0 < n; b0 += lu) {
+                            const u32 t = b0 + sub;
+                            const bool blk =
+                                t < n && mis_blocked_in(a, v, rv, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + t])));
+                            const u32 m = (__ballot_sync(gmask, blk) & gmask) >> gbase;
+                            if (m) {
+                                stop = b0 + (u32)(__ffs(m) - 1);
+                                break;
+                            }
+                        }
+                        if (sub == 0) {
+                            if (stop != NONE) {
+                                a.word[v] = mis_with_resume(rv, stop);
+                                und = true;
+                            } else {
+                                atom_or64(&a.word[v], mis_dec_bits(MIS_IN));
+                                in = true;
+                            }
+                        }
+                    }
+                }
+                mis_queue_warp(qi.small, qi.ns, fi.small, fi.nsmall, in, v);
+                mis_queue_warp(qu.small, qu.ns, fu.small, fu.nsmall, und, v);
+            }
         }
         mis_queue_flush(qu, fu);
         mis_queue_flush(qi, fi);
