@@ -228,6 +228,34 @@ HD u32 wfirst(u32 n, P p) {
     }
     return NONE_IDX;
 }
+// Smallest i in [0, n) with p(i) (NONE_IDX if none), and in kmin the minimum of
+// key(i) over every such i (NONE_IDX if none), in one pass.
+template <class P, class K>
+HD u32 wfirst_min(u32 n, P p, K key, u32& kmin) {
+#if defined(__CUDA_ARCH__)
+    u32 first = NONE_IDX, m = NONE_IDX;
+    for (u32 base = 0; base < n; base += 32) {
+        const u32 i = base + (threadIdx.x & 31u);
+        const bool ok = i < n && p(i);
+        const u32 b = __ballot_sync(kFull, ok);
+        if (first == NONE_IDX && b) first = base + (u32)(__ffs(b) - 1);
+        const u32 k = ok ? key(i) : NONE_IDX;
+        if (k < m) m = k;
+    }
+    kmin = __reduce_min_sync(kFull, m);
+    return first;
+#else
+    u32 first = NONE_IDX, m = NONE_IDX;
+    for (u32 i = 0; i < n; i++) {
+        if (!p(i)) continue;
+        if (first == NONE_IDX) first = i;
+        const u32 k = key(i);
+        if (k < m) m = k;
+    }
+    kmin = m;
+    return first;
+#endif
+}
 // Minimum of f(i) over i in [0, n) (f returns NONE_IDX for "no value").
 template <class F>
 HD u32 wmin(u32 n, F f) {

@@ -21,7 +21,7 @@ constexpr u32 WPV_KL = 384;  // literals per variable
 constexpr u32 WPV_XL = 24;   // XOR literal set (arity <= 20)
 // words per warp slot
 constexpr u32 WPV_HIST = 16;  // original clauses per size (< 16) per list, counted when staging
-constexpr u32 WPV_WORDS = 5 * WPV_KC + WPV_KL + (WPV_KC + 2) + 3 * WPV_XL + 8 + 2 * WPV_HIST;
+constexpr u32 WPV_WORDS = 5 * WPV_KC + WPV_KL + (WPV_KC + 2) + WPV_XL + 8 + 2 * WPV_HIST;
 
 struct WarpPv {
     const Ctx* c;
@@ -34,9 +34,7 @@ struct WarpPv {
     u32* lits;
     u32* out;   // AND/OR fan-in list
     u32* xl;    // XOR literal set
-    u32* xs0;   // list sizes of the XOR literals as staged
-    u32* xs1;   // list sizes of their complements
-    u32* ctl;
+    u32* ctl;   // [side]: original clauses, [2 + side]: their literals (counted when staging)
     u32* hist;  // [side * WPV_HIST + size]
 
     HD void bind(const Ctx& cc, u32* slot) {
@@ -49,9 +47,7 @@ struct WarpPv {
         lits = start + WPV_KC;
         out = lits + WPV_KL;
         xl = out + WPV_KC + 2;
-        xs0 = xl + WPV_XL;
-        xs1 = xs0 + WPV_XL;
-        ctl = xs1 + WPV_XL;
+        ctl = xl + WPV_XL;
         hist = ctl + 8;
     }
     // original clauses of `size` in one side's list (sizes >= WPV_HIST: the list length)
@@ -80,7 +76,7 @@ HD bool wpv_stage(WarpPv& w, const Ctx& c, u32 var) {
     // of the sizes by a warp scan, then the literals from the starts kept in registers
     static_assert(WPV_KC <= 64, "two clauses per lane");
     const u32 lane = threadIdx.x & 31u;
-    u32 gstart[2] = {0, 0}, carry = 0;
+    u32 gstart[2] = {0, 0}, carry = 0, org[2] = {0, 0}, olit[2] = {0, 0};
 #pragma unroll
     for (u32 rr = 0; rr < 2; rr++) {
         const u32 i = rr * 32u + lane;
@@ -94,7 +90,11 @@ HD bool wpv_stage(WarpPv& w, const Ctx& c, u32 var) {
             w.flags[i] = h.flags;
             gstart[rr] = h.start;
             sz = h.size;
-            if (h_original(h.flags) && h.size < WPV_HIST) atomicAdd(&w.hist[(i < np ? 0u : WPV_HIST) + h.size], 1u);
+            if (h_original(h.flags)) {
+                if (h.size < WPV_HIST) atomicAdd(&w.hist[(i < np ? 0u : WPV_HIST) + h.size], 1u);
+                org[i < np ? 0 : 1]++;
+                olit[i < np ? 0 : 1] += h.size;
+            }
         }
         u32 incl = sz;
 #pragma unroll
@@ -104,6 +104,16 @@ HD bool wpv_stage(WarpPv& w, const Ctx& c, u32 var) {
         }
         if (i < tot) w.start[i] = carry + incl - sz;
         carry += __shfl_sync(kFull, incl, 31);
+    }
+    {
+        const u32 o0 = __reduce_add_sync(kFull, org[0]), o1 = __reduce_add_sync(kFull, org[1]);
+        const u32 l0 = __reduce_add_sync(kFull, olit[0]), l1 = __reduce_add_sync(kFull, olit[1]);
+        if (lane == 0) {
+            w.ctl[0] = o0;
+            w.ctl[1] = o1;
+            w.ctl[2] = l0;
+            w.ctl[3] = l1;
+        }
     }
     __syncwarp();
     if (carry > WPV_KL) return false;
@@ -119,6 +129,7 @@ HD bool wpv_stage(WarpPv& w, const Ctx& c, u32 var) {
     __syncwarp();
 #else
     u32 total = 0;
+    for (u32 k = 0; k < 4; k++) w.ctl[k] = 0;
     for (u32 i = 0; i < tot; i++) {
         const u32 r = i < np ? lp[i] : ln[i - np];
         const Hdr h = c.hdr[r];
@@ -128,7 +139,11 @@ HD bool wpv_stage(WarpPv& w, const Ctx& c, u32 var) {
         w.flags[i] = h.flags;
         w.start[i] = total;
         total += h.size;
-        if (h_original(h.flags) && h.size < WPV_HIST) w.hist[(i < np ? 0u : WPV_HIST) + h.size]++;
+        if (h_original(h.flags)) {
+            if (h.size < WPV_HIST) w.hist[(i < np ? 0u : WPV_HIST) + h.size]++;
+            w.ctl[i < np ? 0 : 1]++;
+            w.ctl[i < np ? 2 : 3] += h.size;
+        }
     }
     if (total > WPV_KL) return false;
     for (u32 i = 0; i < tot; i++) {
@@ -162,14 +177,10 @@ HD void wpv_unmelt_if(WarpPv& w, u32 b, u32 e, P pred) {
     });
 }
 
-HD u32 wpv_orgs(const WarpPv& w, u32 side) {
-    const u32 b = w.base(side);
-    return wsum(w.n(side), [&](u32 t) { return h_original(w.flags[b + t]) ? 1u : 0u; });
-}
-HD u32 wpv_lits_before(const WarpPv& w, u32 side) {
-    const u32 b = w.base(side);
-    return wsum(w.n(side), [&](u32 t) { return h_original(w.flags[b + t]) ? w.size[b + t] : 0u; });
-}
+// Original clauses of a side and their literals (fixed while the variable is
+// decided: only molten flags change).
+HD u32 wpv_orgs(const WarpPv& w, u32 side) { return w.ctl[side]; }
+HD u32 wpv_lits_before(const WarpPv& w, u32 side) { return w.ctl[2 + side]; }
 
 // countResolvents / countSubstituted (simplify.h:237-295) over all pairs at once:
 // the rejection test (count > clsbefore, any size above the limit, literal bound)
@@ -233,6 +244,14 @@ HD bool wpv_find_ao_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& n
     const u32 side = dx & 1u, fside = side ^ 1u;
     const u32 b = w.base(side), ns = w.n(side);
     auto is_bin = [&](u32 i) { return h_original(w.flags[i]) && w.size[i] == 2; };
+    // The fan-in is every original binary of the side; the gate needs at least two
+    // and an original clause of one more literal on the other side. Without them the
+    // search below melts the binaries and unmelts them again.
+    const u32 nbin = w.count_size(side, 2);
+    if (nbin < 2 || w.count_size(fside, nbin + 1) == 0) {
+        wpv_unmelt_if(w, b, b + ns, [&](u32 i) { return is_bin(i); });
+        return false;
+    }
     // fan-in literals in list order, binaries melted
     u32 on = 0;
     for (u32 base = 0; base < ns; base += 32) {
@@ -278,28 +297,31 @@ HD bool wpv_find_ao_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& n
     return false;
 }
 
-// fast_equality_check (ifthenelse.h:25-40) on the own list (see pv_fast_equality_check).
+// fast_equality_check (ifthenelse.h:25-40) on the own list (see pv_fast_equality_check):
+// the reference takes the first match in list order when the own literal's list is
+// no longer than the others', else the match of smallest id. The two agree unless
+// two or more clauses match, so the list sizes are only read then.
 HD u32 wpv_feq_lane(const WarpPv& w, u32 x, u32 y, u32 z) {
-    const u32 ownlit = x;
-    u32 sy = w.lsize(y), sz = w.lsize(z);
-    if (sy > sz) { swap_t(y, z); swap_t(sy, sz); }
-    const bool own = !(w.lsize(x) > sy);
     u32 q0 = x, q1 = y, q2 = z;
     { const u32 lo = q1 < q2 ? q1 : q2, hi = q1 < q2 ? q2 : q1; q1 = lo; q2 = hi; }
     { const u32 lo = q0 < q2 ? q0 : q2, hi = q0 < q2 ? q2 : q0; q0 = lo; q2 = hi; }
     { const u32 lo = q0 < q1 ? q0 : q1, hi = q0 < q1 ? q1 : q0; q0 = lo; q1 = hi; }
-    const u32 side = ownlit & 1u, b = w.base(side), e = b + w.n(side);
-    u32 best = NONE, best_id = NONE;
+    const u32 side = x & 1u, b = w.base(side), e = b + w.n(side);
+    u32 first = NONE, best = NONE, best_id = NONE;
     for (u32 i = b; i < e; i++) {
         const u32 f = w.flags[i];
         if (h_molten(f) || !(h_original(f) && w.size[i] == 3)) continue;
         const u32* L = w.L(i);
         if (L[0] == q0 && L[1] == q1 && L[2] == q2) {
-            if (own) return i;
+            if (first == NONE) first = i;
             if (w.id[i] < best_id) { best_id = w.id[i]; best = i; }
         }
     }
-    return best;
+    if (first == best) return first;
+    u32 sy = w.lsize(y);
+    const u32 sz = w.lsize(z);
+    if (sy > sz) sy = sz;
+    return !(w.lsize(x) > sy) ? first : best;
 }
 
 // The ITE candidate pair test of find_ITE_gate (ifthenelse.h:48-70); d1/d2 out.
@@ -359,24 +381,20 @@ HD bool wpv_find_ite_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& 
 }
 
 // makeArity (xor.h:52-84): flip by the next even-parity counter, find the arity
-// clause in the own list (first in order when the reference scans the own list,
-// else the smallest id).
+// clause in the own list: the first in list order when the reference scans the own
+// list (its literal has the shortest list), else the smallest id. The two agree
+// unless two or more clauses match, so the list sizes are only read then.
 HD bool wpv_make_arity(WarpPv& w, u32& parity, u32 size) {
     const u32 oldparity = parity;
     do { ++parity; } while (popc32(parity) & 1);
     wone([&]() {
         for (u32 k = 0; k < size; k++) {
             const u32 bit = 1u << k;
-            if ((parity & bit) != (oldparity & bit)) {
-                w.xl[k] = FLIP(w.xl[k]);
-                swap_t(w.xs0[k], w.xs1[k]);
-            }
+            if ((parity & bit) != (oldparity & bit)) w.xl[k] = FLIP(w.xl[k]);
         }
     });
-    u32 best = w.xl[0], minsize = w.xs0[0], ownlit = w.xl[0];
+    u32 ownlit = w.xl[0];
     for (u32 k = 0; k < size; k++) if (ABS(w.xl[k]) == w.v) ownlit = w.xl[k];
-    for (u32 k = 1; k < size; k++) if (w.xs0[k] < minsize) { minsize = w.xs0[k]; best = w.xl[k]; }
-    const bool own = best == ownlit;
     const u32 side = ownlit & 1u, b = w.base(side), ns = w.n(side);
     auto match = [&](u32 t) {
         const u32 i = b + t;
@@ -389,16 +407,18 @@ HD bool wpv_make_arity(WarpPv& w, u32& parity, u32 size) {
         }
         return true;
     };
-    u32 found;
-    if (own) {
-        const u32 t = wfirst(ns, match);
-        found = t == NONE_IDX ? NONE : b + t;
-    } else {
-        const u32 mid = wmin(ns, [&](u32 t) { return match(t) ? w.id[b + t] : NONE_IDX; });
-        found = NONE;
-        if (mid != NONE_IDX) found = b + wfirst(ns, [&](u32 t) { return w.id[b + t] == mid; });
+    u32 mid = NONE_IDX;
+    const u32 t = wfirst_min(ns, match, [&](u32 q) { return w.id[b + q]; }, mid);
+    if (t == NONE_IDX) return false;
+    u32 found = b + t;
+    if (w.id[found] != mid) {
+        u32 best = w.xl[0], minsize = w.lsize(w.xl[0]);
+        for (u32 k = 1; k < size; k++) {
+            const u32 sk = w.lsize(w.xl[k]);
+            if (sk < minsize) { minsize = sk; best = w.xl[k]; }
+        }
+        if (best != ownlit) found = b + wfirst(ns, [&](u32 q) { return w.id[b + q] == mid; });
     }
-    if (found == NONE) return false;
     wpv_set_molten(w, found, true);
     return true;
 }
@@ -427,12 +447,7 @@ HD bool wpv_find_xor_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& 
             continue;
         }
         frozen = false;  // this candidate's search melts clauses
-        wfor(size, [&](u32 k) {
-            const u32 lit = w.L(i)[k];
-            w.xl[k] = lit;
-            w.xs0[k] = w.lsize(lit);
-            w.xs1[k] = w.lsize(FLIP(lit));
-        });
+        wfor(size, [&](u32 k) { w.xl[k] = w.L(i)[k]; });
         u32 parity = 0;
         int itargets = 1 << arity;
         while (--itargets && wpv_make_arity(w, parity, size)) {}
@@ -485,8 +500,8 @@ HD VeResult wpv_bve_decide(WarpPv& w, const VeOpts& o) {
     r.nlits = adds ? nLits : 0u;
     if (type == VE_KEEP) r.nwit = 0;
     else {
-        const u32 s = pOrgs > nOrgs ? 1u : 0u, bb = w.base(s);
-        r.nwit = 2 + wsum(w.n(s), [&](u32 t) { return h_original(w.flags[bb + t]) ? w.size[bb + t] + 1 : 0u; });
+        const u32 s = pOrgs > nOrgs ? 1u : 0u;
+        r.nwit = 2 + wpv_lits_before(w, s) + wpv_orgs(w, s);
     }
     return r;
 }
