@@ -126,6 +126,19 @@ HD void warp_max_atomic(u32* p, u32 v) {
 #endif
 }
 
+// Sets bit v of a zeroed bitmap when pred holds: the lanes of a warp that share a
+// word combine their bits and one of them ORs the word.
+HD void bitmap_set(u32* bits, u32 v, bool pred) {
+#if defined(__CUDA_ARCH__)
+    const unsigned mask = __activemask();
+    const unsigned peers = __match_any_sync(mask, v >> 5);
+    const u32 b = __reduce_or_sync(peers, pred ? 1u << (v & 31u) : 0u);
+    if (b && (threadIdx.x & 31u) == (u32)(__ffs(peers) - 1)) atomicOr(&bits[v >> 5], b);
+#else
+    if (pred) bits[v >> 5] |= 1u << (v & 31u);
+#endif
+}
+
 // Append to a list through one shared counter: the lanes of a warp that append
 // reserve their slots with one atomic. Returns the slot (only meaningful when pred).
 HD u32 warp_append(u32* counter, bool pred) {

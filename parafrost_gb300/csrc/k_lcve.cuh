@@ -39,6 +39,7 @@ struct LcveArgs {
     u64* word;            // nvars+1: independent-set words
     const Q4* crec;       // per clause: its first three literals and size | deleted << 31
     u64* ws_bytes;        // accumulates the graph's working set (4*occ + sum(8 + 4*len))
+    u32* gbits;           // graph membership, one bit per variable (zeroed before k_mis_init)
     u32* bound;           // per formula f: [2f] = B0 (first valid non-F rank), [2f+1] = B
     const u32* f_active;  // batches: formulas taking part in this election (null: all)
     u32* f_npvs;          // batches: elected variables per formula
@@ -111,6 +112,7 @@ HD void k_mis_init(const LcveArgs& a, const MisFront& und, u32 v) {
     const bool in_graph = v && (!a.f_active || a.f_active[f]) && lcve_valid(a.c, v) && lcve_freezable(a, v) &&
                           a.rank[v] < a.bound[2 * f];
     a.word[v] = in_graph ? a.rank[v] : NONE;
+    bitmap_set(a.gbits, v, in_graph);
     mis_append(und, a.c, v, in_graph);
 }
 
@@ -157,7 +159,10 @@ HD void k_mis_rec(const LcveArgs& a, Q4* rec, u32 i) {
     q.w = h.size | (h_deleted(h.flags) ? 0x80000000u : 0u);
     rec[i] = q;
     u32 ng = 0;
-    for (u32 k = 0; k < h.size; k++) ng += mis_rank(a.word[ABS(l[k])]) != NONE ? 1u : 0u;
+    for (u32 k = 0; k < h.size; k++) {
+        const u32 x = ABS(l[k]);
+        ng += (ldro(&a.gbits[x >> 5]) >> (x & 31u)) & 1u;
+    }
     warp_sum_add64(a.ws_bytes, (u64)ng * (4ull + (h_deleted(h.flags) ? 0ull : 8ull + 4ull * h.size)));
 }
 

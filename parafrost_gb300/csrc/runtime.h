@@ -112,6 +112,15 @@ struct Runtime {
         std::memcpy(d, h, b);
 #endif
     }
+    // queued on the stream; the caller synchronises before reading h
+    void d2h_async(void* h, const void* d, size_t b) {
+        if (!b) return;
+#if SIGMA_CUDA
+        ck(cudaMemcpyAsync(h, d, b, cudaMemcpyDeviceToHost, stream), "d2h");
+#else
+        std::memcpy(h, d, b);
+#endif
+    }
     void d2h(void* h, const void* d, size_t b) {
         if (!b) return;
 #if SIGMA_CUDA

@@ -260,11 +260,13 @@ struct pf_sigma_ctx {
     DBuf<u64> mis_word;
     DBuf<u32> mis_in[4];  // new-in lists of the election rounds (small x2, large x2)
     DBuf<Q4> mis_rec;  // the election's 16-byte clause records
+    DBuf<u32> mis_gbits;  // the election's graph membership bitmap
     DBuf<u32> pv_perm, pv_key;
     DBuf<u32> work, cl_stamp;
     DBuf<u32> radix_hist, radix_hscan, scan_tmp32;
     DBuf<u64> scan_tmp64;
     DBuf<u64> big64a, big64b;
+    DBuf<uint8_t> down_learnt;  // learnt flags of the downloaded clauses
     DBuf<u32> big32a, big32b;
     // BVE
     DBuf<uint8_t> ve_type;
@@ -612,6 +614,9 @@ struct pf_sigma_ctx {
         a.word = mis_word.p;
         mis_rec.reserve(rt, (size_t)ncls + 1);
         a.crec = mis_rec.p;
+        mis_gbits.reserve(rt, (size_t)nvars / 32 + 1);
+        rt.zero(mis_gbits.p, ((size_t)nvars / 32 + 1) * 4);
+        a.gbits = mis_gbits.p;
         a.ws_bytes = counters64.p + 4;
         a.bound = bound.p;
         a.pvs = pvs.p;
@@ -1866,16 +1871,15 @@ pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets
     return guarded([&]() -> pf_status {
         pf_sigma_ctx& c = *ctx;
         if ((lits || offsets || learnt) && c.compact) {
-            // compacted store: the literals are already contiguous in clause order
+            // compacted store: the literals are already contiguous in clause order; all
+            // copies are queued, then one synchronisation
             c.big64a.reserve(c.rt, (size_t)c.ncls + 1);
-            DBuf<uint8_t> lrn;
-            lrn.reserve(c.rt, (size_t)c.ncls + 1);
-            if (c.ncls) c.rt.each(FDownOffsets{c.hdr.p, c.big64a.p, lrn.p}, c.ncls);
+            c.down_learnt.reserve(c.rt, (size_t)c.ncls + 1);
+            if (c.ncls) c.rt.each(FDownOffsets{c.hdr.p, c.big64a.p, c.down_learnt.p}, c.ncls);
             c.write_u64(c.big64a.p + c.ncls, c.nlits_used);
-            if (lits && c.nlits_used) c.rt.d2h(lits, c.lits.p, (size_t)c.nlits_used * 4);
-            if (offsets) c.rt.d2h(offsets, c.big64a.p, ((size_t)c.ncls + 1) * 8);
-            if (learnt && c.ncls) c.rt.d2h(learnt, lrn.p, c.ncls);
-            lrn.free();
+            if (lits && c.nlits_used) c.rt.d2h_async(lits, c.lits.p, (size_t)c.nlits_used * 4);
+            if (offsets) c.rt.d2h_async(offsets, c.big64a.p, ((size_t)c.ncls + 1) * 8);
+            if (learnt && c.ncls) c.rt.d2h_async(learnt, c.down_learnt.p, c.ncls);
         } else if (lits || offsets || learnt) {
             auto H = c.fetch(c.hdr.p, c.ncls);
             std::vector<u32> L;
@@ -1889,9 +1893,10 @@ pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets
             }
             if (offsets) offsets[c.ncls] = o;
         }
-        if (units && c.ntrail) c.rt.d2h(units, c.trail.p, (size_t)c.ntrail * 4);
-        if (resolved && c.nresolved) c.rt.d2h(resolved, c.resolved.p, (size_t)c.nresolved * 4);
-        if (eliminated) c.rt.d2h(eliminated, c.vstate.p, c.nvars + 1);
+        if (units && c.ntrail) c.rt.d2h_async(units, c.trail.p, (size_t)c.ntrail * 4);
+        if (resolved && c.nresolved) c.rt.d2h_async(resolved, c.resolved.p, (size_t)c.nresolved * 4);
+        if (eliminated) c.rt.d2h_async(eliminated, c.vstate.p, c.nvars + 1);
+        c.rt.sync();
         return PF_OK;
     });
 }
@@ -2090,6 +2095,8 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     c.mis_word.free();
     for (auto& b : c.mis_in) b.free();
     c.mis_rec.free();
+    c.mis_gbits.free();
+    c.down_learnt.free();
     c.res_mark.free();
 #if SIGMA_CUDA
     c.scan1_agg.free();

@@ -136,6 +136,26 @@ def occurrence_lists(num_vars: int, lits: np.ndarray, offsets: np.ndarray):
     return off, size, owner[order]
 
 
+class ResultBuffers:
+    """Host buffers reused across Simplifier.result(out=...) calls: each grows to the
+    largest result seen, so repeated downloads write into memory that is already
+    mapped. `alloc(nbytes)` returns a uint8 array (default np.empty); a caller can
+    pass one that returns page-locked memory, which the device copies into directly."""
+
+    def __init__(self, alloc=None):
+        self._alloc = alloc or (lambda n: np.empty(n, dtype=np.uint8))
+        self._bufs: dict = {}
+
+    def take(self, name: str, count: int, dtype) -> np.ndarray:
+        dt = np.dtype(dtype)
+        need = max(int(count), 1) * dt.itemsize
+        b = self._bufs.get(name)
+        if b is None or b.nbytes < need:
+            b = self._alloc(need)
+            self._bufs[name] = b
+        return b[:need].view(dt)[:count]
+
+
 @dataclass
 class Result:
     num_vars: int
@@ -209,16 +229,19 @@ class Simplifier:
         self._check(self.lib.pf_sigma_round(self.h, ctypes.byref(stats)))
         return stats
 
-    def result(self) -> Result:
+    def result(self, out: ResultBuffers | None = None) -> Result:
+        """The simplified formula. With `out`, the arrays are views into its reusable
+        buffers (valid until they are used again); otherwise fresh arrays."""
         nc, nl, nu, nr = _U64(), _U64(), _U64(), _U64()
         self._check(self.lib.pf_sigma_result_sizes(self.h, ctypes.byref(nc), ctypes.byref(nl), ctypes.byref(nu),
                                                    ctypes.byref(nr)))
-        lits = np.empty(nl.value, dtype=np.uint32)
-        offsets = np.empty(nc.value + 1, dtype=np.uint64)
-        learnt = np.empty(nc.value, dtype=np.uint8)
-        units = np.empty(nu.value, dtype=np.uint32)
-        resolved = np.empty(nr.value, dtype=np.uint32)
-        elim = np.empty(self.num_vars + 1, dtype=np.uint8)
+        take = out.take if out is not None else (lambda _name, count, dtype: np.empty(count, dtype=dtype))
+        lits = take("lits", nl.value, np.uint32)
+        offsets = take("offsets", nc.value + 1, np.uint64)
+        learnt = take("learnt", nc.value, np.uint8)
+        units = take("units", nu.value, np.uint32)
+        resolved = take("resolved", nr.value, np.uint32)
+        elim = take("eliminated", self.num_vars + 1, np.uint8)
         self._check(self.lib.pf_sigma_download(self.h, _ptr(lits), _ptr(offsets), _ptr(learnt), _ptr(units),
                                                _ptr(resolved), _ptr(elim)))
         return Result(self.num_vars, lits, offsets, learnt, units, resolved, elim)

@@ -46,3 +46,22 @@ def test_cuda_library_builds_and_exports_every_symbol():
     syms = exported(path)
     missing = [n for n in declared() if n not in syms]
     assert not missing, missing
+
+
+def test_result_into_reused_buffers(built):
+    """result(out=...) returns the same arrays as a fresh download, twice in a row
+    through the same buffers (emulation build)."""
+    import numpy as np
+    from parafrost_gb300 import cnfgen
+    from parafrost_gb300.options import Options
+    from parafrost_gb300.sigma import ResultBuffers, Simplifier
+    nv, lits, off = cnfgen.aig_tseitin(num_inputs=100, num_and=2000, num_xor=200, seed=3)
+    s = Simplifier(Options(all=1), library=built["emu"])
+    buf = ResultBuffers()
+    for _ in range(2):
+        s.awaken(nv, lits, off)
+        s.sigmify()
+        a, b = s.result(), s.result(out=buf)
+        for f in ("lits", "offsets", "learnt", "units", "resolved", "eliminated"):
+            assert np.array_equal(getattr(a, f), getattr(b, f)), f
+    s.close()
