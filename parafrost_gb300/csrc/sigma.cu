@@ -67,7 +67,6 @@ struct FSubRestore { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_rest
 struct FSubReach { SubReachArgs a; const u32* off; u32 nq; HD void operator()(u32 i) const { k_sub_reach(a, off, nq, i); } };
 struct FSubReachSize { Ctx c; const U2* units; u32* size; HD void operator()(u32 q) const { k_sub_reach_size(c, units, size, q); } };
 struct FSubWarp { SubArgs a; HD void operator()(u32 k) const { sub_warp_pv(a, k); } };
-struct FSubSlot { SubArgs a; HD void operator()(u32 k) const { k_sub_slot(a, k); } };
 struct FSubCommit { Ctx c; const u32* lits; HD void operator()(u32 i) const { k_sub_commit_oblivion(c, lits, i); } };
 struct FSubAssign { Ctx c; const U2* units; HD void operator()(u32 i) const { enqueue_unit(c, units[i].y); } };
 struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) const { k_bve_scratch_need(c, pvs, need, i); } };
@@ -734,20 +733,14 @@ struct pf_sigma_ctx {
 
     // One SUB pass over the elected variables (warp per variable).
     void sub_pass(const SubArgs& a) {
-        // staged lists for the exact pass; the passes that can derive units (and
-        // re-runs) touch clauses outside the slot
-        const bool staged = a.cap_units == 0 && !a.pre_off && !a.run;
 #if SIGMA_CUDA
         if (!perm_n) return;
         ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
         rt.launches++;
-        const size_t smem = staged ? 8 * (size_t)SUBW_WORDS * 4 : 0;
-        sub_warp_k<<<(u32)rt.sms * 8u, 256, smem, rt.stream>>>(a, pv_perm.p + perm_off, perm_n, counters.p + 11,
-                                                              staged ? 1 : 0);
+        sub_warp_k<<<(u32)rt.sms * 8u, 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n, counters.p + 11);
         ck(cudaGetLastError(), "launch");
 #else
-        if (staged) pv_each(FSubSlot{a});
-        else pv_each(FSubWarp{a});
+        pv_each(FSubWarp{a});
 #endif
     }
 
