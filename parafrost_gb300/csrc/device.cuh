@@ -110,6 +110,18 @@ HD void warp_sum_add64(u64* p, u64 v) {
 #endif
 }
 
+// Sum into one of kSpreadSlots words chosen by the block (the caller adds the
+// slots up): a sum that every warp of a large launch feeds would otherwise queue
+// all its atomics on one address.
+constexpr u32 kSpreadSlots = 32;
+HD void spread_sum_add64(u64* slots, u64 v) {
+#if defined(__CUDA_ARCH__)
+    warp_sum_add64(slots + (blockIdx.x & (kSpreadSlots - 1u)), v);
+#else
+    slots[0] += v;
+#endif
+}
+
 // Maximum into one word from many threads: one atomic per full warp, and only
 // when the warp's value exceeds what the word already holds (the word settles
 // early, so most warps only read it).

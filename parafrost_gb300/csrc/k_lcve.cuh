@@ -38,7 +38,7 @@ struct LcveArgs {
     u32* rank;            // nvars+1
     u64* word;            // nvars+1: independent-set words
     const Q4* crec;       // per clause: its first three literals and size | deleted << 31
-    u64* ws_bytes;        // accumulates the graph's working set (4*occ + sum(8 + 4*len))
+    u64* ws_bytes;        // kSpreadSlots words summing the graph's working set (4*occ + sum(8 + 4*len))
     u32* gbits;           // graph membership, one bit per variable (zeroed before k_mis_init)
     u32* bound;           // per formula f: [2f] = B0 (first valid non-F rank), [2f+1] = B
     const u32* f_active;  // batches: formulas taking part in this election (null: all)
@@ -163,7 +163,7 @@ HD void k_mis_rec(const LcveArgs& a, Q4* rec, u32 i) {
         const u32 x = ABS(l[k]);
         ng += (ldro(&a.gbits[x >> 5]) >> (x & 31u)) & 1u;
     }
-    warp_sum_add64(a.ws_bytes, (u64)ng * (4ull + (h_deleted(h.flags) ? 0ull : 8ull + 4ull * h.size)));
+    spread_sum_add64(a.ws_bytes, (u64)ng * (4ull + (h_deleted(h.flags) ? 0ull : 8ull + 4ull * h.size)));
 }
 
 // Whether clause cl holds a graph neighbour of v ranked below rv that is not out

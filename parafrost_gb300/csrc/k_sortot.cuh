@@ -32,7 +32,7 @@ struct IdLess {
 struct SortArgs {
     Ctx c;
     const u32* pvs;
-    u64* ws_bytes;  // accumulates the elected lists' working set (4*occ + sum(8 + 4*len))
+    u64* ws_bytes;  // kSpreadSlots words summing the elected lists' working set (4*occ + sum(8 + 4*len))
 };
 
 // One item per list: 2*k is the positive list of pvs[k], 2*k+1 the negative one.
@@ -42,7 +42,7 @@ HD void k_sort_list(const SortArgs& a, u32 k) {
     u32* d = a.c.ot_refs + a.c.ot_off[l];
     u64 ws = 4ull * n;
     for (u32 i = 0; i < n; i++) ws += 8ull + 4ull * a.c.hdr[d[i]].size;
-    warp_sum_add64(a.ws_bytes, ws);
+    spread_sum_add64(a.ws_bytes, ws);
     if (n <= 1) return;
     if (n <= 20) ref_insertion_sort(d, (int)n, IdLess());
     else std_sort_replica(d, d + n, IdLess());

@@ -133,33 +133,51 @@ struct Scan1State {
     u32* err;
 };
 
+// A tile is kScan1Items consecutive items per thread: read once from memory in
+// coalesced order into shared memory, scanned per thread in registers, combined
+// across the block by one warp scan of the thread sums, and written back in
+// coalesced order. Shared-memory positions are padded (one slot per 32) so the
+// per-thread runs of consecutive items do not fall on one bank.
+constexpr int kScan1Items = 16;
+constexpr int kScan1Tile = kScanThreads * kScan1Items;
+__device__ __forceinline__ int scan1_pad(int i) { return i + (i >> 5); }
+
 template <class Tin, class T>
 __global__ void __launch_bounds__(kScanThreads) scan1_k(const Tin* in, T* out, size_t n, T* total, Scan1State st,
                                                        u32 base, u32 epoch) {
-    __shared__ u32 tile_s;
+    __shared__ T items[kScan1Tile + kScan1Tile / 32];
     __shared__ T ws[kScanThreads / 32];
+    __shared__ u32 tile_s;
     __shared__ T carry_s;
     if (threadIdx.x == 0) tile_s = atomicAdd(st.counter, 1u) - base;
     __syncthreads();
     const u32 tile = tile_s;
-    const size_t nb = (n + kScanTile - 1) / kScanTile;
-    const size_t t0 = (size_t)tile * kScanTile;
+    const size_t nb = (n + kScan1Tile - 1) / kScan1Tile;
+    const size_t t0 = (size_t)tile * kScan1Tile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // tile aggregate
-    T s = 0;
-    for (int k = 0; k < kScanItems; k++) {
-        const size_t i = t0 + (size_t)k * kScanThreads + threadIdx.x;
-        if (i < n) s += (T)in[i];
+#pragma unroll
+    for (int k = 0; k < kScan1Items; k++) {
+        const int j = k * kScanThreads + threadIdx.x;
+        const size_t i = t0 + (size_t)j;
+        items[scan1_pad(j)] = i < n ? (T)in[i] : T(0);
     }
-    for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) ws[warp] = s;
+    __syncthreads();
+    // this thread's run: items [threadIdx.x * kScan1Items, +kScan1Items)
+    T run = 0;
+    const int r0 = threadIdx.x * kScan1Items;
+#pragma unroll
+    for (int k = 0; k < kScan1Items; k++) run += items[scan1_pad(r0 + k)];
+    const T incl = warp_incl_scan(run);
+    if (lane == 31) ws[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-        // warp 0 publishes the aggregate and looks back 32 tiles at a time: it waits
-        // for their flags, adds the aggregates after the nearest inclusive prefix and
-        // stops there (or moves 32 tiles further back)
-        T a = 0;
-        for (int w = 0; w < kScanThreads / 32; w++) a += ws[w];
+        // block aggregate and per-warp offsets, then the look-back (as before, 32
+        // tiles at a time: wait for their flags, add the aggregates after the
+        // nearest inclusive prefix and stop there)
+        T wv = lane < kScanThreads / 32 ? ws[lane] : T(0);
+        const T winc = warp_incl_scan(wv);
+        const T a = __shfl_sync(0xffffffffu, winc, kScanThreads / 32 - 1);
+        if (lane < kScanThreads / 32) ws[lane] = winc - wv;
         T prefix = 0;
         if (lane == 0) {
             if (tile == 0) st.incl[0] = (u64)a;
@@ -185,7 +203,6 @@ __global__ void __launch_bounds__(kScanThreads) scan1_k(const Tin* in, T* out, s
             late = __any_sync(0xffffffffu, late);
             if (late) break;
             __threadfence();
-            // lanes 0.. look at tiles top, top-1, ...: the first inclusive one stops the walk
             const u32 incl_mask = __ballot_sync(0xffffffffu, p >= 0 && (f & 3u) == 2u);
             const int stop = incl_mask ? __ffs(incl_mask) - 1 : 32;
             T v = 0;
@@ -208,26 +225,25 @@ __global__ void __launch_bounds__(kScanThreads) scan1_k(const Tin* in, T* out, s
         }
     }
     __syncthreads();
-    for (int k = 0; k < kScanItems; k++) {
-        const size_t i = t0 + (size_t)k * kScanThreads + threadIdx.x;
-        const T v = i < n ? (T)in[i] : T(0);
-        const T incl = warp_incl_scan(v);
-        if (lane == 31) ws[warp] = incl;
-        __syncthreads();
-        T wpre = 0, btot = 0;
-        for (int w = 0; w < kScanThreads / 32; w++) {
-            if (w < warp) wpre += ws[w];
-            btot += ws[w];
-        }
-        const T carry = carry_s;
-        if (i < n) out[i] = carry + wpre + incl - v;
-        __syncthreads();
-        if (threadIdx.x == 0) carry_s = carry + btot;
-        __syncthreads();
+    // exclusive prefixes of this thread's run, in place
+    T acc = carry_s + ws[warp] + incl - run;
+#pragma unroll
+    for (int k = 0; k < kScan1Items; k++) {
+        const int q = scan1_pad(r0 + k);
+        const T v = items[q];
+        items[q] = acc;
+        acc += v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScan1Items; k++) {
+        const int j = k * kScanThreads + threadIdx.x;
+        const size_t i = t0 + (size_t)j;
+        if (i < n) out[i] = items[scan1_pad(j)];
     }
 }
 
-inline size_t scan1_tiles(size_t n) { return (n + kScanTile - 1) / kScanTile; }
+inline size_t scan1_tiles(size_t n) { return (n + kScan1Tile - 1) / kScan1Tile; }
 
 // ---------------------------------------------------------------- radix sort
 constexpr int kRadixThreads = 256;

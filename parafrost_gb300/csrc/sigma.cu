@@ -253,7 +253,8 @@ struct pf_sigma_ctx {
     DBuf<uint8_t> vstate;
     DBuf<u32> trail, resolved;
     DBuf<u32> counters;   // [0] ntrail, [1] err, [2..] scratch counters
-    DBuf<u64> counters64; // [0] nresolved, [1] elected working set, [2..3] counts, [4] graph working set
+    DBuf<u64> counters64; // [0] nresolved, [2..3] counts
+    DBuf<u64> ws_slots;   // [0, 32): elected lists' working set, [32, 64): graph working set (summed slots)
     // stage scratch
     DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
     DBuf<u32> mis_big_a, mis_big_b;
@@ -350,6 +351,13 @@ struct pf_sigma_ctx {
         u32 v = 0;
         rt.d2h(&v, d, 4);
         return v;
+    }
+    u64 read_slots(const u64* d) {
+        u64 v[kSpreadSlots];
+        rt.d2h(v, d, sizeof v);
+        u64 t = 0;
+        for (u64 x : v) t += x;
+        return t;
     }
     u64 read_u64(const u64* d) {
         u64 v = 0;
@@ -617,7 +625,7 @@ struct pf_sigma_ctx {
         mis_gbits.reserve(rt, (size_t)nvars / 32 + 1);
         rt.zero(mis_gbits.p, ((size_t)nvars / 32 + 1) * 4);
         a.gbits = mis_gbits.p;
-        a.ws_bytes = counters64.p + 4;
+        a.ws_bytes = ws_slots.p + kSpreadSlots;
         a.bound = bound.p;
         a.pvs = pvs.p;
         a.f_active = nf ? f_active.p : nullptr;
@@ -708,8 +716,8 @@ struct pf_sigma_ctx {
     }
 
     void sort_ot() {
-        rt.zero(counters64.p + 1, 8);
-        SortArgs a{view(), pvs.p, counters64.p + 1};
+        rt.zero(ws_slots.p, kSpreadSlots * 8);
+        SortArgs a{view(), pvs.p, ws_slots.p};
         rt.each(FSortList{a}, 2 * npvs);
         // work order of the per-variable kernels: most clauses first (longest
         // processing time first), so similar variables share a warp and the longest
@@ -729,7 +737,7 @@ struct pf_sigma_ctx {
     }
 
     // working set of the elected lists, accumulated by the sort kernel
-    u64 pv_bytes() { return read_u64(counters64.p + 1); }
+    u64 pv_bytes() { return read_slots(ws_slots.p); }
 
     // One SUB pass over the elected variables (warp per variable).
     void sub_pass(const SubArgs& a) {
@@ -1796,7 +1804,8 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     }
     pf_status status = PF_OK;
     try {
-        c.rt.zero(c.counters64.p + 4, 8);
+        c.ws_slots.reserve(c.rt, 2 * kSpreadSlots);
+        c.rt.zero(c.ws_slots.p + kSpreadSlots, kSpreadSlots * 8);
         pf_options& o = c.opt;
         if (c.opt.dump_level > 0) {
             c.dump_cnf(0, 0);
@@ -1840,7 +1849,7 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     if (status == PF_OK || status == PF_UNSAT) {
         try {
             c.rt.sync();
-            c.kbytes[pf_sigma_ctx::K_MIS] = c.read_u64(c.counters64.p + 4);
+            c.kbytes[pf_sigma_ctx::K_MIS] = c.read_slots(c.ws_slots.p + kSpreadSlots);
             for (int k = 0; k < pf_sigma_ctx::K_COUNT; k++) {
                 c.st.ms_kernel[k] = c.kclock[k].total_ms();
                 c.st.bytes_kernel[k] = c.kbytes[k];
@@ -2088,7 +2097,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
                         &c.sub_ent, &c.sub_ent_off, &c.sub_ids, &c.sub_words, &c.sub_sizes, &c.sub_pre_off,
                         &c.sub_pre_lits, &c.sub_ulits, &c.ere_target, &c.ere_losers};
     for (auto* b : b32) b->free();
-    DBuf<u64>* b64[] = {&c.counters64, &c.scan_tmp64, &c.big64a, &c.big64b, &c.ve_scr_off, &c.ve_lit_scan,
+    DBuf<u64>* b64[] = {&c.counters64, &c.ws_slots, &c.scan_tmp64, &c.big64a, &c.big64b, &c.ve_scr_off, &c.ve_lit_scan,
                         &c.ve_wit_scan, &c.sub_wrd, &c.sub_wrd_off, &c.ere_claim, &c.ere_key};
     for (auto* b : b64) b->free();
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
