@@ -342,6 +342,39 @@ struct pf_sigma_ctx {
         return c;
     }
 
+    // Values the host needs together (scan totals, counters, the error word) are
+    // gathered into device slots on the stream and read back with one copy, so a
+    // stage waits for the device once instead of once per value.
+    DBuf<u64> hread;
+    u64 hr[8] = {};
+    u64* hslot(int k) {
+        hread.reserve(rt, 8);
+        return hread.p + k;
+    }
+    // scan with its total into slot k
+    template <class Tin, class T>
+    void scan_to(const Tin* in, T* out, size_t n, int k) {
+#if SIGMA_CUDA
+        rt.zero(hslot(k), 8);
+        scan1_launch(in, out, n, (T*)hslot(k));
+#else
+        u64 t;
+        if constexpr (sizeof(T) == 4) t = scan32(in, out, n);
+        else t = scan64(in, out, n);
+        rt.h2d(hslot(k), &t, 8);
+#endif
+    }
+    // a device word into slot k (zero-extended)
+    void word_to(const u32* d, int k) {
+        rt.zero(hslot(k), 8);
+        rt.d2d(hslot(k), d, 4);
+    }
+    // all slots into hr; the error word rides along in slot 7 and is checked
+    void read_slots_checked(u32 stage_err_mask = ~0u) {
+        word_to(counters.p + 1, 7);
+        rt.d2h(hr, hslot(0), 8 * sizeof(u64));
+        check_err((u32)hr[7] & stage_err_mask);
+    }
     u32 read_err() {
         u32 e = 0;
         rt.d2h(&e, counters.p + 1, 4);
@@ -390,6 +423,16 @@ struct pf_sigma_ctx {
     u32 scan1_epoch = 0, scan1_base = 0;
     template <class Tin, class T>
     T scan1(const Tin* in, T* out, size_t n) {
+        scan1_total.reserve(rt, 2);
+        T* total = (T*)scan1_total.p;
+        scan1_launch(in, out, n, total);
+        T h = 0;
+        rt.d2h(&h, total, sizeof(T));
+        return h;
+    }
+    // the scan, its total written to the device word `total` (no synchronisation)
+    template <class Tin, class T>
+    void scan1_launch(const Tin* in, T* out, size_t n, T* total) {
         const size_t tiles = scan1_tiles(n);
         if (!scan1_ctl.p || scan1_base > 0x7FFFFFFFu || scan1_epoch >= 0x3FFFFFFFu) {
             scan1_ctl.reserve(rt, 4);
@@ -405,8 +448,6 @@ struct pf_sigma_ctx {
             scan1_flag.reserve(rt, cap);
             rt.zero(scan1_flag.p, scan1_flag.bytes());
         }
-        scan1_total.reserve(rt, 2);
-        T* total = (T*)scan1_total.p;
         if (n == 0) {
             rt.zero(total, sizeof(T));
         } else {
@@ -417,9 +458,6 @@ struct pf_sigma_ctx {
             ck(cudaGetLastError(), "launch");
             scan1_base += (u32)tiles;
         }
-        T h = 0;
-        rt.d2h(&h, total, sizeof(T));
-        return h;
     }
     u32 scan32(const u32* in, u32* out, size_t n) { return scan1<u32, u32>(in, out, n); }
     template <class Tin>
@@ -498,8 +536,8 @@ struct pf_sigma_ctx {
         rec(6, ph, 3, d);
     }
 
-    void check(u32 stage_err_mask = ~0u) {
-        const u32 e = read_err() & stage_err_mask;
+    void check(u32 stage_err_mask = ~0u) { check_err(read_err() & stage_err_mask); }
+    void check_err(u32 e) {
         if (e & ERR_UNSAT) throw int(PF_UNSAT);
         if (e & (ERR_CAP_CLAUSES | ERR_CAP_LITS | ERR_CAP_WITNESS | ERR_CAP_SCRATCH)) throw std::runtime_error("capacity exceeded (internal sizing bug)");
         if (e & ERR_ITER) throw int(PF_ETIMEOUT);
@@ -535,13 +573,20 @@ struct pf_sigma_ctx {
         Ctx c = view();
         rt.zero(ot_size.p, (size_t)D * 4);
         rt.each(FHist{c}, ncls);
-        const u32 total = scan32(ot_size.p, ot_off.p, D);
-        write_u32(ot_off.p + D, total);
-        if (total > ot_refs.n) ot_refs.reserve(rt, (size_t)total + total / 4 + 1024);
+        // the occurrences (live clauses' literals) never exceed the literal pool in
+        // use, so the table is sized before its total is known
+        if (nlits_used > ot_refs.n) ot_refs.reserve(rt, (size_t)nlits_used + nlits_used / 4 + 1024);
+#if SIGMA_CUDA
+        scan1_launch(ot_size.p, ot_off.p, D, ot_off.p + D);
+#else
+        write_u32(ot_off.p + D, scan32(ot_size.p, ot_off.p, D));
+#endif
         rt.d2d(ot_cursor.p, ot_off.p, (size_t)D * 4);
         c = view();
         rt.each(FScatter{c}, ncls);
-        check();
+        word_to(ot_off.p + D, 0);
+        read_slots_checked();
+        const u32 total = (u32)hr[0];
         ot_dirty = false;
         alg_bytes += 2ull * (4ull * nlits_used + 8ull * ncls) + 8ull * D + 4ull * total;
     }
@@ -676,8 +721,6 @@ struct pf_sigma_ctx {
            "cooperative launch");
         kclock[K_MIS].stop(rt);
         rt.launches++;
-        check();
-        rounds = read_u32(ctr + 14);
 #else
         MisFront und[2] = {{flags.p, ctr, mis_big_a.p, ctr + 1}, {flags_scan.p, ctr + 4, mis_big_b.p, ctr + 5}};
         MisFront ins[2] = {{mis_in[0].p, ctr + 2, mis_in[2].p, ctr + 3}, {mis_in[1].p, ctr + 6, mis_in[3].p, ctr + 7}};
@@ -695,13 +738,23 @@ struct pf_sigma_ctx {
         }
         kclock[K_MIS].stop(rt);
 #endif
-        mis_rounds += rounds;
         rt.each(FBoundInit{a}, nform);
         rt.each(FMisBound{a}, nvars + 1);
         rt.each(FFill32{pvrank.p, NONE}, nvars + 1);
         rt.each(FElectFlag{a, flags.p}, nvars);
         if (nf) rt.zero(f_npvs.p, (size_t)nf * 4);
-        npvs = scan32(flags.p, flags_scan.p, nvars);
+        // one read: the elected count, the rounds run and the error word (a round
+        // that ran out of time is caught here; the kernels since only read words)
+        scan_to(flags.p, flags_scan.p, nvars, 0);
+#if SIGMA_CUDA
+        word_to(ctr + 14, 1);
+#endif
+        read_slots_checked();
+        npvs = (u32)hr[0];
+#if SIGMA_CUDA
+        rounds = (u32)hr[1];
+#endif
+        mis_rounds += rounds;
         rt.each(FElectWrite{a, flags.p, flags_scan.p}, nvars);
         n_go = npvs;
         perm_off = 0;
@@ -957,10 +1010,12 @@ struct pf_sigma_ctx {
         kclock[K_BVE].stop(rt);
 #endif
         kbytes[K_BVE] += phase_ws;
-        check();
-        const u32 add_cls = scan32(ve_ncls.p, ve_cls_scan.p, npvs);
-        const u64 add_lits = scan64(ve_nlits.p, ve_lit_scan.p, npvs);
-        const u64 add_wit = scan64(ve_nwit.p, ve_wit_scan.p, npvs);
+        scan_to(ve_ncls.p, ve_cls_scan.p, npvs, 0);
+        scan_to(ve_nlits.p, ve_lit_scan.p, npvs, 1);
+        scan_to(ve_nwit.p, ve_wit_scan.p, npvs, 2);
+        read_slots_checked();
+        const u32 add_cls = (u32)hr[0];
+        const u64 add_lits = hr[1], add_wit = hr[2];
         ensure_clauses((u64)ncls + add_cls);
         ensure_lits(nlits_used + add_lits);
         ensure_resolved(nresolved + add_wit);
@@ -988,8 +1043,9 @@ struct pf_sigma_ctx {
         ncls += add_cls;
         nlits_used += add_lits;
         nresolved += add_wit;
-        ntrail = read_u32(counters.p + 0);
-        check();
+        word_to(counters.p + 0, 0);
+        read_slots_checked();
+        ntrail = (u32)hr[0];
         alg_bytes += 4ull * add_lits + 8ull * add_cls + 4ull * add_wit;
     }
 
@@ -1109,8 +1165,11 @@ struct pf_sigma_ctx {
         big64b.reserve(rt, (size_t)ncls + 1);
         Ctx c = view();
         rt.each(FGcFlags{c, big32a.p, big64a.p}, ncls);
-        const u32 keep = scan32(big32a.p, big32b.p, ncls);
-        const u64 keep_lits = scan64(big64a.p, big64b.p, ncls);
+        scan_to(big32a.p, big32b.p, ncls, 0);
+        scan_to(big64a.p, big64b.p, ncls, 1);
+        read_slots_checked();
+        const u32 keep = (u32)hr[0];
+        const u64 keep_lits = hr[1];
         hdr2.reserve(rt, hdr.n);
         lits2.reserve(rt, std::max<size_t>(lits.n, (size_t)keep_lits + 16));
         GcArgs g{c, big32b.p, big64b.p, hdr2.p, lits2.p};
