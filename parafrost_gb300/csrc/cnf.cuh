@@ -77,9 +77,18 @@ struct Ctx {
     const u32* var_fid;
     u32* f_err;
     uint8_t* res_mark;  // batches: 1 on the last word (the length) of every witness record
+    // per clause: the phase stamp of its last change of literals or status
+    // (deletion and creation included), and this phase's stamp
+    u32* cstamp;
+    u32 stamp;
 };
 
 constexpr u32 NONE = 0xFFFFFFFFu;
+
+// Clause r's literals or status changed in this phase.
+HD void touch(const Ctx& c, u32 r) {
+    if (c.cstamp) c.cstamp[r] = c.stamp;
+}
 
 HD int lit_value(const Ctx& c, u32 lit) {
     const u32 a = vload(&c.asg[ABS(lit)]);

@@ -49,6 +49,11 @@ struct BveArgs {
     u32 cls_base;
     u64 lit_base;
     u64 wit_base;
+    // per variable: the stamp of its last KEEP decision (0: none) and the lists it
+    // saw then (positive size | negative size << 8 | originals << 16, << 24);
+    // null: every variable is decided
+    u32* keep_at;
+    u32* keep_shape;
 };
 
 struct ListRef {
@@ -82,7 +87,43 @@ HD bool merge_into(u32 x, const u32* a, u32 n1, const u32* b, u32 n2, u32* out, 
 
 // Step 1 with one warp per elected variable (k_bve_warp.cuh); variables too large
 // for the warp slot take the per-thread decision on lane 0.
+// A variable decided KEEP whose two lists have the same sizes and whose clauses
+// have not changed since (no clause stamped after that decision: every change of
+// literals or status, deletion included, stamps the clause, and a clause that joins
+// a list is new or changed) sees the same lists in the same order (lists are
+// rebuilt and sorted from the same clauses in the same store order), and decides
+// KEEP again: the decision depends on
+// the lists' clauses and order alone (other literals' list sizes only pick between
+// identical matches of a gate, which KEEP does not use). Its result is written
+// without staging the lists.
+HD bool bve_keep_again(const BveArgs& a, u32 k) {
+    if (!a.keep_at) return false;
+    const Ctx& c = a.c;
+    const u32 v = a.pvs[k];
+    const u32 at = a.keep_at[v];
+    if (!at) return false;
+    const u32 p = V2L(v), np = c.ot_size[p], nn = c.ot_size[p + 1];
+    const u32 sh = a.keep_shape[v];
+    if ((sh & 0xFFu) != np || ((sh >> 8) & 0xFFu) != nn) return false;
+    const u32* lp = c.ot_refs + c.ot_off[p];
+    const u32* ln = c.ot_refs + c.ot_off[p + 1];
+    const u32 changed = wsum(np + nn, [&](u32 i) { return c.cstamp[i < np ? lp[i] : ln[i - np]] > at ? 1u : 0u; });
+    if (changed) return false;
+    if (lane_id() == 0) {
+        a.type[k] = VE_KEEP;
+        a.porgs[k] = (sh >> 16) & 0xFFu;
+        a.norgs[k] = sh >> 24;
+        a.def[k] = 0;
+        a.ncls[k] = 0;
+        a.nlits[k] = 0;
+        a.nwit[k] = 0;
+    }
+    wsync();
+    return true;
+}
+
 HD void bve_warp_one(const BveArgs& a, u32 k, u32* slot) {
+    if (bve_keep_again(a, k)) return;
     VeOpts o;
     o.ve_clause_max = a.ve_clause_max;
     o.ve_lbound = a.ve_lbound;
@@ -105,6 +146,12 @@ HD void bve_warp_one(const BveArgs& a, u32 k, u32* slot) {
         a.ncls[k] = r.ncls;
         a.nlits[k] = r.nlits;
         a.nwit[k] = r.nwit;
+        if (a.keep_at) {
+            const u32 v = a.pvs[k];
+            const bool keep = staged && r.type == VE_KEEP;
+            a.keep_at[v] = keep ? a.c.stamp : 0u;
+            if (keep) a.keep_shape[v] = w.np | (w.nn << 8) | (r.porgs << 16) | (r.norgs << 24);
+        }
     }
     wsync();
 }
@@ -197,6 +244,7 @@ HD u32 substitute_clause(const Ctx& c, u32 r, u32 dx, u32 def) {
         else if (lit != def) l[n++] = lit;
     }
     h.size = n;
+    touch(c, r);
     if (n == 1) { c.hdr[r].size = 1; return l[0]; }
     reference_list_sort(l, (int)n, LitLess());
     h.sig = calc_sig(l, n);
@@ -283,6 +331,7 @@ HD void k_bve_write(const BveArgs& a, u32 k) {
                     nh.sig = calc_sig(c.lits + ls, on);
                     nh.flags = ST_ORIGINAL | F_ADDED;
                     c.hdr[id] = nh;
+                    touch(c, id);
                     id++;
                     ls += on;
                 }
@@ -361,6 +410,7 @@ __device__ void bve_write_warp(const BveArgs& a, u32 k) {
                 nh.sig = calc_sig(c.lits + my_ls, on);
                 nh.flags = ST_ORIGINAL | F_ADDED;
                 c.hdr[my_id] = nh;
+                touch(c, my_id);
             }
         }
         id += (u32)__popc(kept);

@@ -76,6 +76,7 @@ HD void prop_lists(const PropArgs& a, u32 k) {
     for (u32 i = 0; i < ts; i++) {
         const u32 r = c.ot_refs[to + i];
         c.hdr[r].flags = (ldw<Fresh>(&c.hdr[r].flags) & ~3u) | ST_DELETED;
+        touch(c, r);
     }
     c.ot_size[t] = 0;
     c.ot_size[f] = 0;
@@ -105,6 +106,7 @@ HD void prop_clause(const PropArgs& a, u32 k) {
         for (u32 j = 0; j < PROP_SHORT; j++) sat |= val[j] == 1;
         if (sat) {
             c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+            touch(c, r);
             return;
         }
 #pragma unroll
@@ -119,6 +121,7 @@ HD void prop_clause(const PropArgs& a, u32 k) {
         for (u32 i = 0; i < h.size; i++) {
             if (lit_value(c, ldw<Fresh>(&l[i])) == 1) {
                 c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+                touch(c, r);
                 return;
             }
         }
@@ -132,10 +135,14 @@ HD void prop_clause(const PropArgs& a, u32 k) {
     h.size = n;
     h.sig = sig;
     c.hdr[r] = h;
+    touch(c, r);
     if (n == 0) {
         set_unsat(c, v0);
         // in a batch the other formulas go on: keep no empty live clause around
-        if (c.var_fid) c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+        if (c.var_fid) {
+            c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+            touch(c, r);
+        }
         return;
     }
     if (n == 1) {
@@ -173,6 +180,7 @@ DEV void prop_lists_warp(const PropArgs& a, u32 k) {
     for (u32 i = lane; i < ts; i += 32) {
         const u32 r = c.ot_refs[to + i];
         c.hdr[r].flags = (__ldcg(&c.hdr[r].flags) & ~3u) | ST_DELETED;
+        touch(c, r);
     }
     __syncwarp();
     if (lane == 0) {

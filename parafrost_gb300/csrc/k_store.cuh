@@ -220,6 +220,7 @@ struct GcArgs {
     const u64* lit_scan;     // exclusive scan of kept sizes
     Hdr* new_hdr;
     u32* new_lits;
+    u32* new_stamp;  // the clause stamps move with the headers
 };
 HD void k_gc_flags(const Ctx& c, u32* keep, u64* sizes, u32 i) {
     const Hdr h = c.hdr[i];
@@ -235,6 +236,7 @@ HD void k_gc_move(const GcArgs& a, u32 i) {
     Hdr nh = h;
     nh.start = (u32)st;
     a.new_hdr[id] = nh;
+    if (a.c.cstamp) a.new_stamp[id] = a.c.cstamp[i];
     const u32* src = a.c.lits + h.start;
     u32* dst = a.new_lits + st;
     for (u32 k = 0; k < h.size; k++) dst[k] = src[k];

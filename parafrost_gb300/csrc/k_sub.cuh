@@ -69,7 +69,10 @@ HD bool sorted_has(const u32* l, u32 n, u32 lit) {
     return lo < n && l[lo] == lit;
 }
 
-HD void mark_deleted(const Ctx& c, u32 r) { c.hdr[r].flags = (c.hdr[r].flags & ~3u) | ST_DELETED; }
+HD void mark_deleted(const Ctx& c, u32 r) {
+    c.hdr[r].flags = (c.hdr[r].flags & ~3u) | ST_DELETED;
+    touch(c, r);
+}
 HD void set_molten(const Ctx& c, u32 r, bool m) {
     const u32 f = c.hdr[r].flags;
     c.hdr[r].flags = m ? (f | F_MOLTEN) : (f & ~F_MOLTEN);
@@ -122,6 +125,7 @@ HD void sub_strengthen(const SubArgs& a, u32 k, u32 p, u32 r, u32 me, SubLocal& 
     h.size = h.size - 1;
     c.hdr[r].sig = h.sig;
     c.hdr[r].size = h.size;
+    touch(c, r);
     if (n == 1) {
         const u32 unit = l[0];
         int val = lit_value(c, unit);
@@ -152,7 +156,10 @@ HD bool sub_subsume(const Ctx& c, const u32* list, u32 end, u32 cr) {
         if (h_deleted(s.flags)) continue;
         if (h_molten(cand.flags) && s.size > cand.size) continue;
         if (s.size > 1 && sig_sub(s.sig, cand.sig) && clause_sub(c.lits + s.start, s.size, cl, cand.size)) {
-            if (h_learnt(s.flags) && h_original(cand.flags)) c.hdr[sr].flags = (s.flags & ~3u) | ST_ORIGINAL;
+            if (h_learnt(s.flags) && h_original(cand.flags)) {
+                c.hdr[sr].flags = (s.flags & ~3u) | ST_ORIGINAL;
+                touch(c, sr);
+            }
             mark_deleted(c, cr);
             return true;
         }
@@ -313,6 +320,7 @@ HD void k_sub_restore(const SubCkptArgs& a, u32 k) {
             e++;
             c.ot_refs[o + i] = r;
             c.hdr[r] = h;
+            touch(c, r);
             for (u32 t = 0; t < h.size; t++) c.lits[h.start + t] = a.words[w++];
         }
     }

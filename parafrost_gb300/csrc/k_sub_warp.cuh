@@ -55,7 +55,10 @@ HD void sub_warp_side(const SubArgs& a, u32 k, u32 p, u32 lx, u32 lo, SubLocal& 
             wone([&] {
                 const u32 sr = cands[jb];
                 const Hdr s = c.hdr[sr];
-                if (h_learnt(s.flags) && h_original(cand.flags)) c.hdr[sr].flags = (s.flags & ~3u) | ST_ORIGINAL;
+                if (h_learnt(s.flags) && h_original(cand.flags)) {
+                    c.hdr[sr].flags = (s.flags & ~3u) | ST_ORIGINAL;
+                    touch(c, sr);
+                }
                 mark_deleted(c, r);
             });
         }

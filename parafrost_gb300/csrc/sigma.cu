@@ -245,6 +245,8 @@ struct pf_sigma_ctx {
     u32 wave_stamp = 0;
     // clause store (double-buffered for compaction)
     DBuf<Hdr> hdr, hdr2;
+    DBuf<u32> cstamp, cstamp2;  // per clause: phase stamp of its last change (Ctx::cstamp)
+    DBuf<u32> keep_at, keep_shape;  // per variable: the last KEEP decision (BveArgs)
     DBuf<u32> lits, lits2;
     // occurrence table
     DBuf<u32> ot_off, ot_size, ot_refs, ot_cursor;
@@ -339,6 +341,8 @@ struct pf_sigma_ctx {
         c.var_fid = nf ? var_fid.p : nullptr;
         c.f_err = nf ? f_err.p : nullptr;
         c.res_mark = nf ? res_mark.p : nullptr;
+        c.cstamp = cstamp.p;
+        c.stamp = (u32)phase + 1u;
         return c;
     }
 
@@ -551,6 +555,7 @@ struct pf_sigma_ctx {
         const size_t cap = (size_t)(need + need / 4 + 1024);
         if (cap > 0xFFFFFFF0ull) throw OomError("clause count exceeds 32-bit ids");
         hdr.grow(rt, cap, ncls);
+        cstamp.grow(rt, cap, ncls);
     }
     void ensure_lits(u64 need) {
         if (need <= lits.n) return;
@@ -989,6 +994,8 @@ struct pf_sigma_ctx {
         a.def = ve_def.p;
         a.scr_off = ve_scr_off.p;
         a.scr = ve_scr.p;
+        a.keep_at = keep_at.p;
+        a.keep_shape = keep_shape.p;
 #if SIGMA_CUDA
         {
             const int smem = kBveWarpThreads / 32 * (int)WPV_WORDS * 4;
@@ -1171,10 +1178,12 @@ struct pf_sigma_ctx {
         const u32 keep = (u32)hr[0];
         const u64 keep_lits = hr[1];
         hdr2.reserve(rt, hdr.n);
+        cstamp2.reserve(rt, hdr.n);
         lits2.reserve(rt, std::max<size_t>(lits.n, (size_t)keep_lits + 16));
-        GcArgs g{c, big32b.p, big64b.p, hdr2.p, lits2.p};
+        GcArgs g{c, big32b.p, big64b.p, hdr2.p, lits2.p, cstamp2.p};
         rt.each(FGcMove{g}, ncls);
         std::swap(hdr, hdr2);
+        std::swap(cstamp, cstamp2);
         std::swap(lits, lits2);
         alg_bytes += (4ull * nlits_used + 8ull * ncls) + (4ull * keep_lits + 8ull * keep);
         ncls = keep;
@@ -1661,6 +1670,8 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         const size_t cap_cls = (size_t)num_clauses + num_clauses / 2 + 1024;
         const size_t cap_lits = (size_t)L + L / 2 + 4096;
         c.hdr.reserve(rt, cap_cls);
+        c.cstamp.reserve(rt, cap_cls);
+        rt.zero(c.cstamp.p, cap_cls * 4);
         c.lits.reserve(rt, cap_lits);
         c.cl_stamp.reserve(rt, cap_cls);
         rt.zero(c.cl_stamp.p, cap_cls * 4);
@@ -1863,6 +1874,9 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     }
     pf_status status = PF_OK;
     try {
+        c.keep_at.reserve(c.rt, (size_t)c.nvars + 1);
+        c.keep_shape.reserve(c.rt, (size_t)c.nvars + 1);
+        c.rt.zero(c.keep_at.p, ((size_t)c.nvars + 1) * 4);
         c.ws_slots.reserve(c.rt, 2 * kSpreadSlots);
         c.rt.zero(c.ws_slots.p + kSpreadSlots, kSpreadSlots * 8);
         pf_options& o = c.opt;
@@ -2154,9 +2168,10 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
                         &c.radix_hist, &c.radix_hscan, &c.scan_tmp32, &c.big32a, &c.big32b, &c.ve_porgs,
                         &c.ve_norgs, &c.ve_ncls, &c.ve_nlits, &c.ve_nwit, &c.ve_def, &c.ve_cls_scan, &c.ve_scr,
                         &c.sub_ent, &c.sub_ent_off, &c.sub_ids, &c.sub_words, &c.sub_sizes, &c.sub_pre_off,
-                        &c.sub_pre_lits, &c.sub_ulits, &c.ere_target, &c.ere_losers};
+                        &c.sub_pre_lits, &c.sub_ulits, &c.ere_target, &c.ere_losers, &c.cstamp, &c.cstamp2,
+                        &c.keep_at, &c.keep_shape};
     for (auto* b : b32) b->free();
-    DBuf<u64>* b64[] = {&c.counters64, &c.ws_slots, &c.scan_tmp64, &c.big64a, &c.big64b, &c.ve_scr_off, &c.ve_lit_scan,
+    DBuf<u64>* b64[] = {&c.counters64, &c.ws_slots, &c.hread, &c.scan_tmp64, &c.big64a, &c.big64b, &c.ve_scr_off, &c.ve_lit_scan,
                         &c.ve_wit_scan, &c.sub_wrd, &c.sub_wrd_off, &c.ere_claim, &c.ere_key};
     for (auto* b : b64) b->free();
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
