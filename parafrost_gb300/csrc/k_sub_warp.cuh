@@ -87,7 +87,7 @@ HD void sub_warp_pv(const SubArgs& a, u32 k) {
 constexpr u32 kSubWarpChunk = 4;
 
 // Warps take elected variables in work order (perm), a few at a time.
-__global__ void __launch_bounds__(256) sub_warp_k(SubArgs a, const u32* perm, u32 n, u32* next) {
+__global__ void __launch_bounds__(256, 8) sub_warp_k(SubArgs a, const u32* perm, u32 n, u32* next) {
     const u32 lane = threadIdx.x & 31u;
     while (true) {
         u32 j0 = 0;
