@@ -280,8 +280,9 @@ class Simplifier:
                                                           d_lits, d_offsets))
         self.batch_vars = num_vars.copy()
 
-    def batch_results(self) -> list:
-        """[(status, phases, Result)] per formula of the last batched round."""
+    def batch_results(self, out: ResultBuffers | None = None) -> list:
+        """[(status, phases, Result)] per formula of the last batched round. With
+        `out`, the arrays are views into its reusable buffers."""
         nf = self.batch_vars.size
         st = np.empty(nf, dtype=np.int32)
         ph = np.empty(nf, dtype=np.uint32)
@@ -289,12 +290,13 @@ class Simplifier:
         self._check(self.lib.pf_sigma_batch_result_sizes(self.h, _ptr(st), _ptr(ph), _ptr(nc), _ptr(nl), _ptr(nu),
                                                          _ptr(nr)))
         C, Lt, U, R = int(nc.sum()), int(nl.sum()), int(nu.sum()), int(nr.sum())
-        lits = np.empty(Lt, dtype=np.uint32)
-        offsets = np.empty(C + 1, dtype=np.uint64)
-        learnt = np.empty(C, dtype=np.uint8)
-        units = np.empty(U, dtype=np.uint32)
-        resolved = np.empty(R, dtype=np.uint32)
-        elim = np.empty(int(self.batch_vars.astype(np.uint64).sum()) + nf, dtype=np.uint8)
+        take = out.take if out is not None else (lambda _name, count, dtype: np.empty(count, dtype=dtype))
+        lits = take("lits", Lt, np.uint32)
+        offsets = take("offsets", C + 1, np.uint64)
+        learnt = take("learnt", C, np.uint8)
+        units = take("units", U, np.uint32)
+        resolved = take("resolved", R, np.uint32)
+        elim = take("eliminated", int(self.batch_vars.astype(np.uint64).sum()) + nf, np.uint8)
         self._check(self.lib.pf_sigma_batch_download(self.h, _ptr(lits), _ptr(offsets), _ptr(learnt), _ptr(units),
                                                      _ptr(resolved), _ptr(elim)))
         out = []

@@ -7,7 +7,7 @@ import pytest
 import oracle_runner as orr
 from parafrost_gb300 import cnfgen, rounddump as rd
 from parafrost_gb300.options import Options
-from parafrost_gb300.sigma import PF_EINVAL, SigmaError, Simplifier
+from parafrost_gb300.sigma import PF_EINVAL, ResultBuffers, SigmaError, Simplifier
 
 
 def mixed_batch(seed: int, n: int = 14) -> list:
@@ -35,7 +35,10 @@ def check_batch(lib, forms, opts, oracle=True):
     b.awaken_batch(forms)
     b.sigmify()
     got = b.batch_results()
+    again = b.batch_results(out=ResultBuffers())  # the same through reused buffers
     b.close()
+    for (st, _, res), (st2, _, res2) in zip(got, again):
+        assert rd.canonical_result(st, res if st == 0 else None) == rd.canonical_result(st2, res2 if st2 == 0 else None)
     assert len(got) == len(forms)
     for i, ((nv, lits, off), (st, ph, res)) in enumerate(zip(forms, got)):
         s = Simplifier(opts, library=lib)
