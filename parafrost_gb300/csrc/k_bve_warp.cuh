@@ -10,8 +10,6 @@
 // exceed the slot run the per-thread decision (k_bve_analyze.cuh) on lane 0.
 #pragma once
 
-#include <cmath>
-
 #include "cnf.cuh"
 #include "introsort.cuh"
 #include "k_bve_analyze.cuh"
@@ -219,7 +217,7 @@ HD bool wpv_count_added(const WarpPv& w, const VeOpts& o, int clsbefore, u32 sme
 HD u32 wpv_find_bn_gate(WarpPv& w) {
     const u32 p = V2L(w.v), n = NEG(p);
     auto is_bin = [&](u32 i) { return h_original(w.flags[i]) && w.size[i] == 2; };
-    const u32 nb = w.count_size(0, 2);  // original binaries of the positive list
+    const u32 nb = wsum(w.np, [&](u32 i) { return is_bin(i) ? 1u : 0u; });
     if (nb == 1) {
         const u32 bi = wfirst(w.np, [&](u32 i) { return is_bin(i); });
         const u32* l = w.L(bi);
@@ -348,69 +346,38 @@ HD bool wpv_ite_pair(const WarpPv& w, u32 dx, u32 i, u32 j, u32& d1, u32& d2) {
     return d2 != NONE;
 }
 
-// Pair t of the m(m-1)/2 pairs (x, y), x < y < m, in (x, y) order: row x starts at
-// x(2m - x - 1)/2. The square root gives the row up to rounding; the integer steps
-// settle it.
-HD void tri_pair(u32 m, u32 t, u32& x, u32& y) {
-    auto row0 = [&](u32 r) { return r * (2u * m - r - 1u) / 2u; };
-    const float b = (float)(2u * m - 1u);
-    const float disc = b * b - 8.0f * (float)t;
-#if defined(__CUDA_ARCH__)
-    const float r = (b - sqrtf(disc > 0.0f ? disc : 0.0f)) * 0.5f;
-#else
-    const float r = (b - std::sqrt(disc > 0.0f ? disc : 0.0f)) * 0.5f;
-#endif
-    u32 xr = r > 0.0f ? (u32)r : 0u;
-    if (xr > m - 2u) xr = m - 2u;  // rows 0 .. m-2
-    while (xr > 0 && row0(xr) > t) xr--;
-    while (xr + 1u <= m - 2u && row0(xr + 1u) <= t) xr++;
-    x = xr;
-    y = xr + 1u + (t - row0(xr));
-}
-
-// find_ITE_gate (ifthenelse.h:42-97): first successful pair in (i, j) order. Only
-// pairs of original ternary clauses can succeed, so the search runs over the pairs
-// of those (their positions collected in w.out), all pairs spread over the lanes
-// at once; the first hit in pair order is the reference's first hit.
+// find_ITE_gate (ifthenelse.h:42-97): first successful pair in (i, j) order.
 HD bool wpv_find_ite_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& nAdded, u32& nLits) {
     const u32 side = dx & 1u, b = w.base(side), ns = w.n(side);
-    const u32 m = w.count_size(side, 3);
     // a gate needs a pair of original ternary clauses in this list; without one the
     // search below fails with no effect
-    if (m < 2) return false;
-    for (u32 base = 0, at = 0; base < ns; base += 32) {
-        const u32 msk = wballot([&](u32 l) { return base + l < ns && h_original(w.flags[b + base + l]) && w.size[b + base + l] == 3; });
-        const u32 at0 = at;
-        wfor(32, [&](u32 l) {
-            if ((msk >> l) & 1u) w.out[at0 + (u32)popc32(msk & ((1u << l) - 1u))] = b + base + l;
+    if (w.count_size(side, 3) < 2) return false;
+    for (u32 a = 0; a < ns; a++) {
+        const u32 i = b + a;
+        if (!(h_original(w.flags[i]) && w.size[i] == 3)) continue;
+        const u32 t = wfirst(ns - a - 1, [&](u32 q) {
+            u32 d1, d2;
+            return wpv_ite_pair(w, dx, i, i + 1 + q, d1, d2);
         });
-        at += (u32)popc32(msk);
+        if (t == NONE_IDX) continue;
+        const u32 j = i + 1 + t;
+        u32 d1 = NONE, d2 = NONE;
+        wpv_ite_pair(w, dx, i, j, d1, d2);
+        wpv_set_molten(w, i, true);
+        wpv_set_molten(w, j, true);
+        wpv_set_molten(w, d1, true);
+        wpv_set_molten(w, d2, true);
+        nAdded = 0;
+        if (wpv_count_added(w, o, nOrgCls, side, nAdded, nLits, true)) {
+            wpv_set_molten(w, i, false);
+            wpv_set_molten(w, j, false);
+            wpv_set_molten(w, d1, false);
+            wpv_set_molten(w, d2, false);
+            return false;
+        }
+        return true;
     }
-    const u32 P = m * (m - 1u) / 2u;
-    const u32 t = wfirst(P, [&](u32 q) {
-        u32 x, y, d1, d2;
-        tri_pair(m, q, x, y);
-        return wpv_ite_pair(w, dx, w.out[x], w.out[y], d1, d2);
-    });
-    if (t == NONE_IDX) return false;
-    u32 x, y;
-    tri_pair(m, t, x, y);
-    const u32 i = w.out[x], j = w.out[y];
-    u32 d1 = NONE, d2 = NONE;
-    wpv_ite_pair(w, dx, i, j, d1, d2);
-    wpv_set_molten(w, i, true);
-    wpv_set_molten(w, j, true);
-    wpv_set_molten(w, d1, true);
-    wpv_set_molten(w, d2, true);
-    nAdded = 0;
-    if (wpv_count_added(w, o, nOrgCls, side, nAdded, nLits, true)) {
-        wpv_set_molten(w, i, false);
-        wpv_set_molten(w, j, false);
-        wpv_set_molten(w, d1, false);
-        wpv_set_molten(w, d2, false);
-        return false;
-    }
-    return true;
+    return false;
 }
 
 // makeArity (xor.h:52-84): flip by the next even-parity counter, find the arity
@@ -466,76 +433,19 @@ HD bool wpv_find_xor_gate(WarpPv& w, const VeOpts& o, u32 dx, int nOrgCls, int& 
     // candidate whose size has fewer originals than that in either list cannot
     // complete; its search would only melt and then unmelt clauses longer than two,
     // which freeze_arities does directly (once while nothing melts in between).
-    auto candidate = [&](u32 i) {
-        if (!h_original(w.flags[i])) return false;
-        const u32 size = w.size[i];
-        const int arity = (int)size - 1;
-        if (size < 3 || arity > o.xor_max_arity) return false;
-        const u32 need = arity - 1 < 31 ? (1u << (arity - 1)) : 0xFFFFFFFFu;
-        return w.count_size(side, size) >= need && w.count_size(side ^ 1u, size) >= need;
-    };
-    // The first makeArity step of every candidate at once: flipping its first two
-    // literals must give a clause of the list of the flipped own literal. A
-    // candidate that fails it melts nothing, like one the counts reject. Candidates
-    // (positions in w.out) and their pass bits (w.ctl[4..5]) in list order.
-    u32 nc = 0;
-    for (u32 base = 0; base < ns; base += 32) {
-        const u32 msk = wballot([&](u32 l) { return base + l < ns && candidate(b + base + l); });
-        const u32 nc0 = nc;
-        wfor(32, [&](u32 l) {
-            if ((msk >> l) & 1u) w.out[nc0 + (u32)popc32(msk & ((1u << l) - 1u))] = b + base + l;
-        });
-        nc += (u32)popc32(msk);
-    }
-    if (!nc) {
-        // no candidate passes the counts: the reference's search only freezes
-        if (ns && wfirst(ns, [&](u32 a) {
-                const u32 i = b + a;
-                return h_original(w.flags[i]) && w.size[i] >= 3 && (int)w.size[i] - 1 <= o.xor_max_arity;
-            }) != NONE_IDX)
-            freeze_arities();
-        return false;
-    }
-    wone([&]() { w.ctl[4] = w.ctl[5] = 0; });
-    {
-        const u32 lmax = w.np > w.nn ? w.np : w.nn;
-        wfor(nc * lmax, [&](u32 q) {
-            const u32 c = q / lmax, t = q % lmax;
-            const u32 i = w.out[c], size = w.size[i];
-            const u32* L = w.L(i);
-            const u32 ts = (L[0] == dx || L[1] == dx) ? side ^ 1u : side;
-            if (t >= w.n(ts)) return;
-            const u32 j = w.base(ts) + t;
-            if (!(h_original(w.flags[j]) && w.size[j] == size)) return;
-            const u32* M = w.L(j);
-            for (u32 a2 = 0; a2 < size; a2++) {
-                bool in = M[a2] == FLIP(L[0]) || M[a2] == FLIP(L[1]);
-                for (u32 q2 = 2; q2 < size && !in; q2++) in = M[a2] == L[q2];
-                if (!in) return;
-            }
-#if defined(__CUDA_ARCH__)
-            atomicOr(&w.ctl[4 + (c >> 5)], 1u << (c & 31u));
-#else
-            w.ctl[4 + (c >> 5)] |= 1u << (c & 31u);
-#endif
-        });
-    }
     bool frozen = false;
-    u32 c = 0;
     for (u32 a = 0; a < ns; a++) {
         const u32 i = b + a;
         if (!h_original(w.flags[i])) continue;
         const u32 size = w.size[i];
         const int arity = (int)size - 1;
         if (size < 3 || arity > o.xor_max_arity) continue;
-        const bool counted = candidate(i);
-        if (!counted || !((w.ctl[4 + (c >> 5)] >> (c & 31u)) & 1u)) {
-            c += counted ? 1u : 0u;
+        const u32 need = arity - 1 < 31 ? (1u << (arity - 1)) : 0xFFFFFFFFu;
+        if (w.count_size(side, size) < need || w.count_size(side ^ 1u, size) < need) {
             if (!frozen) freeze_arities();  // a repeat would change nothing
             frozen = true;
             continue;
         }
-        c++;
         frozen = false;  // this candidate's search melts clauses
         wfor(size, [&](u32 k) { w.xl[k] = w.L(i)[k]; });
         u32 parity = 0;
