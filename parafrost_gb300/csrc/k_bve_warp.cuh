@@ -217,7 +217,7 @@ HD bool wpv_count_added(const WarpPv& w, const VeOpts& o, int clsbefore, u32 sme
 HD u32 wpv_find_bn_gate(WarpPv& w) {
     const u32 p = V2L(w.v), n = NEG(p);
     auto is_bin = [&](u32 i) { return h_original(w.flags[i]) && w.size[i] == 2; };
-    const u32 nb = wsum(w.np, [&](u32 i) { return is_bin(i) ? 1u : 0u; });
+    const u32 nb = w.count_size(0, 2);  // original binaries of the positive list
     if (nb == 1) {
         const u32 bi = wfirst(w.np, [&](u32 i) { return is_bin(i); });
         const u32* l = w.L(bi);
