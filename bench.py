@@ -209,9 +209,9 @@ def run_reference(args) -> dict:
 NCU_NAMES = {"mis_rounds": "mis_rounds_k", "bve_decide": "bve_warp_k", "sub": "sub_warp_k", "bve_write": "bve_write_warp_k"}
 
 
-def profiled_traffic(kernel: str, workload: str):
-    """DRAM bytes per launch (read + write) of `kernel` on `workload`, from the
-    committed ncu summary profiles/dram_traffic.txt ('traffic:' lines), or None."""
+def profiled_line(kernel: str, workload: str):
+    """The 'traffic:' line of `kernel` on `workload` in the committed ncu summary
+    profiles/dram_traffic.txt, as a dict, or None."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
     try:
         with open(path) as f:
@@ -220,10 +220,29 @@ def profiled_traffic(kernel: str, workload: str):
                     continue
                 kv = dict(x.split("=", 1) for x in line.split()[1:])
                 if kv.get("kernel") == NCU_NAMES.get(kernel) and kv.get("workload") == workload:
-                    return float(kv["bytes_per_launch"])
-    except (OSError, ValueError, KeyError):
+                    return kv
+    except (OSError, ValueError):
         pass
     return None
+
+
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch (read + write) of `kernel` on `workload`, or None."""
+    kv = profiled_line(kernel, workload)
+    try:
+        return float(kv["bytes_per_launch"]) if kv else None
+    except (KeyError, ValueError):
+        return None
+
+
+def profiled_utilisation(kernel: str, workload: str):
+    """SM and DRAM throughput (% of peak) of the profiled launch, or None: what bounds
+    a kernel whose algorithmic bytes are far below the copy peak."""
+    kv = profiled_line(kernel, workload)
+    if not kv or "sm_pct" not in kv:
+        return None
+    return {"sm_throughput_pct": float(kv["sm_pct"]), "dram_throughput_pct": float(kv["dram_pct"]),
+            "launch": kv.get("measured_launch"), "source": "profiles/dram_traffic.txt (ncu --set full)"}
 
 
 def flush_l2(buf):
@@ -342,6 +361,7 @@ def run_ours(args) -> dict:
     dom = max(kern, key=lambda k: kern[k]["ms_per_step"])
     achieved = kern[dom]["gbs"] or 0.0
     traffic = profiled_traffic(dom, args.workload)
+    util = profiled_utilisation(dom, args.workload)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
@@ -356,7 +376,8 @@ def run_ours(args) -> dict:
                         "frac": achieved / peak, "traffic": traffic, "kernel": dom,
                         "algorithmic_bytes_per_launch": kern[dom]["bytes_per_launch"],
                         "ms_per_launch": kern[dom]["ms_per_launch"],
-                        "peak_source": "MEASURED_PEAKS.json (hbm_gbs, of measured)" if peaks else "fallback"},
+                        "peak_source": "MEASURED_PEAKS.json (hbm_gbs, of measured)" if peaks else "fallback",
+                        "ncu_utilisation": util},
            "kernels": kern,
            "round_roofline": {"achieved": round_gbs, "frac": round_gbs / peak,
                               "scope": "whole round: algorithmic bytes / round device time"},
