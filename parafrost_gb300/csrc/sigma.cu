@@ -831,7 +831,10 @@ struct pf_sigma_ctx {
             kclock[K_SUB].start(rt);
             sub_pass(a);
             kclock[K_SUB].stop(rt);
-            check();
+            // the exact pass derives no unit; its error word is read with the next
+            // stage's values (the VE preparation and the counts only read the store)
+            // unless stage dumps are being recorded
+            if (opt.dump_level) check();
             return;
         }
         sub_safe(a);
@@ -976,7 +979,9 @@ struct pf_sigma_ctx {
         ve_wit_scan.reserve(rt, npvs);
         big64a.reserve(rt, npvs + 1);
         rt.each(FBveNeed{c, pvs.p, big64a.p}, npvs);
-        const u64 scr_words = scan64(big64a.p, ve_scr_off.p, npvs);
+        scan_to(big64a.p, ve_scr_off.p, npvs, 0);
+        read_slots_checked();
+        const u64 scr_words = hr[0];
         ve_scr.reserve(rt, (size_t)scr_words + 16);
         BveArgs a;
         a.c = c;
@@ -1076,7 +1081,9 @@ struct pf_sigma_ctx {
 #else
         pv_each(FBceCountWarp{a});
 #endif
-        const u64 add = scan64(ve_nwit.p, ve_wit_scan.p, npvs);
+        scan_to(ve_nwit.p, ve_wit_scan.p, npvs, 0);
+        read_slots_checked();
+        const u64 add = hr[0];
         if (!add) return;
         ensure_resolved(nresolved + add);
         a.c = view();
@@ -1154,10 +1161,10 @@ struct pf_sigma_ctx {
 #else
         rt.each(FCount{a}, ncls);
 #endif
-        u64 h[2];
-        rt.d2h(h, counters64.p + 2, 16);
-        n_cls_after = (i64)h[0];
-        n_lits_after = (i64)h[1];
+        rt.d2d(hslot(0), counters64.p + 2, 16);
+        read_slots_checked();
+        n_cls_after = (i64)hr[0];
+        n_lits_after = (i64)hr[1];
     }
 
     // shrinkSimp (simplify.cpp:234-245).
