@@ -11,7 +11,8 @@
 // frozen and its lists are necessarily long) or an independent-set member whose
 // lists reach the temperatures. The independent set is the greedy one in rank
 // order (a vertex joins when every lower-ranked neighbour is out, leaves when one
-// lower-ranked neighbour is in), decided by frontier waves over the graph.
+// lower-ranked neighbour is in), decided by push/pull rounds over the graph
+// (mis_rounds_k below).
 #pragma once
 
 #include "cnf.cuh"
