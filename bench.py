@@ -588,6 +588,7 @@ def run_ours_serve(args) -> dict:
             "config": {"workload": args.workload, "pool": len(pool),
                        "pool_clauses": int(sum(f[2].size - 1 for f in pool)), "requests_per_rate": per_rate,
                        "rates": list(SERVE_RATES), "hbm_budget_bytes": budget,
+                       "workers": {"batched": 2, "plain": 1},
                        "timing": "wall clock from scheduled arrival to result on host"},
             "sweep": sweep, "admitted_hbm_bytes": max(r["max_footprint_bytes"] for r in sweep),
             "e2e": {"value": value, "unit": SERVE_UNIT,

@@ -1,12 +1,15 @@
 """Serving loop: simplification requests arrive over time and are answered by
 batched sigmify rounds on one GPU.
 
-A request is one formula. The server thread takes every request that is waiting
-when the GPU becomes free, admits them in arrival order while their estimated
-device footprint fits the HBM budget (and the batch's formula cap), and runs one
-batched round over them (``pf_sigma_upload_batch`` -> ``pf_sigma_round`` ->
-``pf_sigma_batch_download``): each formula gets exactly the result of its own
-round. In ``plain`` mode every request runs alone through the single-formula
+A request is one formula. A worker thread takes every request that is waiting
+when it becomes free, admits them in arrival order while their estimated device
+footprint fits its share of the HBM budget (and the batch's formula cap), and
+runs one batched round over them (``pf_sigma_upload_batch`` -> ``pf_sigma_round``
+-> ``pf_sigma_batch_download``): each formula gets exactly the result of its own
+round. Batched mode runs two workers, each with its own context and stream, so one
+batch's copies and host work overlap the other's kernels on the device, and
+requests that arrive while a batch runs are admitted as soon as a worker is free.
+In ``plain`` mode one worker runs every request alone through the single-formula
 calls instead, the comparison point for batching. Latency is measured from a
 request's arrival to the moment its result is on the host.
 
@@ -57,10 +60,11 @@ class Request:
 
 
 class Server:
-    """One GPU, one server thread, requests answered in arrival order."""
+    """One GPU; worker threads (two in batched mode, one in plain mode), each with
+    its own context; requests admitted in arrival order."""
 
     def __init__(self, opts: Options | None = None, hbm_budget: int = 64 << 30, max_batch: int = 4096,
-                 mode: str = "batched", library: str | None = None):
+                 mode: str = "batched", library: str | None = None, workers: int | None = None):
         if mode not in ("batched", "plain"):
             raise ValueError("mode is 'batched' or 'plain'")
         self.opts = opts or Options(all=1)
@@ -68,34 +72,38 @@ class Server:
         self.max_batch = int(max_batch)
         self.mode = mode
         self.library = library
+        self.workers = int(workers) if workers else (2 if mode == "batched" else 1)
+        self.worker_budget = self.hbm_budget // self.workers
         self.q: queue.Queue = queue.Queue()
         self.batches: list = []          # (formulas, clauses, estimated bytes, device bytes held after, launches)
-        self._launches = 0
-        self.max_footprint = 0
+        self.max_footprint = 0           # device bytes held by all workers' contexts at once, at most
+        self._held: list = [0] * self.workers
+        self._lock = threading.Lock()
         self._stop = threading.Event()
-        self._thread: threading.Thread | None = None
+        self._threads: list = []
         self._pending: list = []
 
     # ---- client side
     def submit(self, formula: tuple, arrival: float | None = None) -> Request:
         r = Request(formula, time.perf_counter() if arrival is None else arrival)
         nv, lits, off = formula
-        if estimate_footprint(nv, off.size - 1, lits.size) > self.hbm_budget:
+        if estimate_footprint(nv, off.size - 1, lits.size) > self.worker_budget:
             self._finish(r, -2, error="request larger than the HBM budget")
             return r
         self.q.put(r)
         return r
 
     def start(self) -> "Server":
-        self._thread = threading.Thread(target=self._run, name="sigma-server", daemon=True)
-        self._thread.start()
+        for w in range(self.workers):
+            t = threading.Thread(target=self._run, args=(w,), name=f"sigma-server-{w}", daemon=True)
+            t.start()
+            self._threads.append(t)
         return self
 
     def stop(self, timeout: float | None = None) -> None:
         self._stop.set()
-        self.q.put(None)
-        if self._thread:
-            self._thread.join(timeout)
+        for t in self._threads:
+            t.join(timeout)
 
     def __enter__(self):
         return self.start()
@@ -110,83 +118,84 @@ class Server:
         r.done.set()
 
     def _admit(self) -> list:
-        """The next batch: waiting requests in arrival order while they fit."""
+        """The next batch (called under the lock): waiting requests in arrival order
+        while they fit one worker's budget; [] once stopped with nothing waiting."""
         reqs = self._pending
         self._pending = []
-        if not reqs:
-            first = self.q.get()
-            if first is None:
+        while not reqs:
+            if self._stop.is_set() and self.q.empty():
                 return []
-            reqs = [first]
+            try:
+                r = self.q.get(timeout=0.02)
+            except queue.Empty:
+                continue
+            reqs = [r]
         while True:
             try:
-                r = self.q.get_nowait()
+                reqs.append(self.q.get_nowait())
             except queue.Empty:
                 break
-            if r is None:
-                self._stop.set()
-                break
-            reqs.append(r)
         batch, used = [], 0
         for i, r in enumerate(reqs):
             nv, lits, off = r.formula
             need = estimate_footprint(nv, off.size - 1, lits.size)
-            if batch and (used + need > self.hbm_budget or len(batch) >= self.max_batch):
+            if batch and (used + need > self.worker_budget or len(batch) >= self.max_batch):
                 self._pending = reqs[i:]
                 break
             batch.append(r)
             used += need
         return batch
 
-    def _run(self) -> None:
+    def _run(self, w: int) -> None:
         ctx = Simplifier(self.opts, library=self.library)
         try:
             while True:
-                if self._stop.is_set() and not self._pending and self.q.empty():
-                    break
-                batch = self._admit()
+                with self._lock:
+                    batch = self._admit()
+                    bi = len(self.batches)
+                    if batch:
+                        self.batches.append(None)  # this batch's slot, filled below
                 if not batch:
-                    if self._stop.is_set():
-                        break
-                    continue
-                bi = len(self.batches)
-                self._launches = 0
+                    break
+                launches = 0
                 if self.mode == "plain":
                     for r in batch:
-                        self._serve_one(ctx, r, bi)
+                        launches += self._serve_one(ctx, r, bi)
                 else:
-                    self._serve_batch(ctx, batch, bi)
+                    launches = self._serve_batch(ctx, batch, bi)
                 fp = ctx.footprint()
-                self.max_footprint = max(self.max_footprint, fp)
                 est = sum(estimate_footprint(r.formula[0], r.formula[2].size - 1, r.formula[1].size) for r in batch)
-                self.batches.append((len(batch), int(sum(r.formula[2].size - 1 for r in batch)), est, fp,
-                                     self._launches))
+                with self._lock:
+                    self._held[w] = fp
+                    self.max_footprint = max(self.max_footprint, sum(self._held))
+                    self.batches[bi] = (len(batch), int(sum(r.formula[2].size - 1 for r in batch)), est, fp, launches)
         finally:
             ctx.close()
 
-    def _serve_one(self, ctx: Simplifier, r: Request, bi: int) -> None:
+    def _serve_one(self, ctx: Simplifier, r: Request, bi: int) -> int:
         nv, lits, off = r.formula
         try:
             ctx.awaken(nv, lits, off)
             st = ctx.sigmify()
-            self._launches += st.kernel_launches
             self._finish(r, st.status, st.phases_run, ctx.result() if st.status == 0 else None, batch=bi)
+            return st.kernel_launches
         except Exception as e:  # the request fails, the server goes on
             self._finish(r, getattr(e, "status", -4), error=str(e), batch=bi)
+            return 0
 
-    def _serve_batch(self, ctx: Simplifier, batch: list, bi: int) -> None:
+    def _serve_batch(self, ctx: Simplifier, batch: list, bi: int) -> int:
         forms = [r.formula for r in batch]
         try:
             ctx.awaken_batch(forms)
             st = ctx.sigmify()
-            self._launches += st.kernel_launches
             out = ctx.batch_results()
         except Exception as e:
             for r in batch:
                 self._finish(r, getattr(e, "status", -4), error=str(e), batch=bi)
-            return
-        for r, (st, ph, res) in zip(batch, out):
-            self._finish(r, st, ph, res if st == 0 else None, batch=bi)
+            return 0
+        for r, (st_f, ph, res) in zip(batch, out):
+            self._finish(r, st_f, ph, res if st_f == 0 else None, batch=bi)
+        return st.kernel_launches
 
 
 def poisson_load(server: Server, pool: list, rate: float, num: int, seed: int = 1) -> list:
