@@ -344,6 +344,45 @@ HD void k_bve_write(const BveArgs& a, u32 k) {
 }
 
 #if SIGMA_CUDA
+// oblivion_var over the lanes: the saved list's original clauses get their witness
+// records at offsets from a warp prefix of their lengths (the sequential loop's
+// order), every clause of both lists is deleted, and the variable's own witness
+// closes the records.
+__device__ void oblivion_var_warp(const Ctx& c, u32 p, u32 pOrgs, u32 nOrgs, u64 w) {
+    const u32 lane = threadIdx.x & 31u;
+    const u32 n = NEG(p);
+    const u32 save = pOrgs > nOrgs ? n : p;
+    const u32 other = pOrgs > nOrgs ? p : n;
+    const ListRef S = list_of(c, save);
+    for (u32 b0 = 0; b0 < S.n; b0 += 32u) {
+        const u32 i = b0 + lane;
+        u32 r = 0, words = 0;
+        Hdr h;
+        if (i < S.n) {
+            r = S.ids[i];
+            h = c.hdr[r];
+            words = h_original(h.flags) ? h.size + 1u : 0u;
+        }
+        u64 incl = words;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u64 t = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o) incl += t;
+        }
+        if (words) save_clause(c, w + incl - words, c.lits + h.start, h.size, save);
+        if (i < S.n) mark_deleted(c, r);
+        w += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    const ListRef O = list_of(c, other);
+    for (u32 i = lane; i < O.n; i += 32u) mark_deleted(c, O.ids[i]);
+    __syncwarp();
+    if (lane == 0) {
+        save_witness(c, w, pOrgs > nOrgs ? p : n);
+        c.ot_size[save] = 0;
+        c.ot_size[other] = 0;
+    }
+}
+
 // Step 2 with one warp per elected variable: the resolvent pairs, in the
 // reference's (i, j) order, go over the lanes 32 at a time; a warp prefix of the
 // kept ones gives each its id and literal offset, so the clauses land where the
@@ -416,19 +455,19 @@ __device__ void bve_write_warp(const BveArgs& a, u32 k) {
         id += (u32)__popc(kept);
         ls += __shfl_sync(0xffffffffu, incl, 31);
     }
-    bad = __any_sync(0xffffffffu, bad);
+    bad = __any_sync(0xffffffffu, bad) || id != id_end || ls != ls_end;
     __syncwarp();
-    if (lane == 0) {
-        if (bad || id != id_end || ls != ls_end) set_err(c, ERR_INTERNAL);
-        else {
-            oblivion_var(c, p, a.porgs[k], a.norgs[k], a.wit_base + a.wit_scan[k]);
-            c.vstate[v] = 1;  // markEliminated (src/cpu/solve.h:535-541)
-        }
+    if (bad) {
+        if (lane == 0) set_err(c, ERR_INTERNAL);
+        __syncwarp();
+        return;
     }
+    oblivion_var_warp(c, p, a.porgs[k], a.norgs[k], a.wit_base + a.wit_scan[k]);
+    if (lane == 0) c.vstate[v] = 1;  // markEliminated (src/cpu/solve.h:535-541)
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(256) bve_write_warp_k(BveArgs a, const u32* perm, u32 npos, u32* next) {
+__global__ void __launch_bounds__(256, 5) bve_write_warp_k(BveArgs a, const u32* perm, u32 npos, u32* next) {
     const u32 lane = threadIdx.x & 31u;
     while (true) {
         u32 j0 = 0;
