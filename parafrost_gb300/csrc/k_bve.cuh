@@ -159,7 +159,7 @@ HD void bve_warp_one(const BveArgs& a, u32 k, u32* slot) {
 #if SIGMA_CUDA
 constexpr int kBveWarpThreads = 256;
 constexpr u32 kBveWarpChunk = 4;  // variables a warp takes per counter increment
-__global__ void __launch_bounds__(kBveWarpThreads) bve_warp_k(BveArgs a, const u32* perm, u32* next) {
+__global__ void __launch_bounds__(kBveWarpThreads, 6) bve_warp_k(BveArgs a, const u32* perm, u32* next) {
     extern __shared__ u32 smem[];
     u32* slot = smem + (threadIdx.x >> 5) * WPV_WORDS;
     const u32 lane = threadIdx.x & 31u;
