@@ -467,7 +467,7 @@ __device__ void bve_write_warp(const BveArgs& a, u32 k) {
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(256, 5) bve_write_warp_k(BveArgs a, const u32* perm, u32 npos, u32* next) {
+__global__ void __launch_bounds__(256, 6) bve_write_warp_k(BveArgs a, const u32* perm, u32 npos, u32* next) {
     const u32 lane = threadIdx.x & 31u;
     while (true) {
         u32 j0 = 0;
