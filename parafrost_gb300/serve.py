@@ -147,7 +147,16 @@ class Server:
         return batch
 
     def _run(self, w: int) -> None:
-        ctx = Simplifier(self.opts, library=self.library)
+        try:
+            ctx = Simplifier(self.opts, library=self.library)
+        except Exception as e:  # no context: this worker answers what it admits with the error
+            while True:
+                with self._lock:
+                    batch = self._admit()
+                if not batch:
+                    return
+                for r in batch:
+                    self._finish(r, getattr(e, "status", -4), error=str(e))
         try:
             while True:
                 with self._lock:

@@ -83,3 +83,14 @@ def test_serve_gpu(cuda_lib, mode):
         want, ph = own_round(cuda_lib, f, opts)
         assert rd.canonical_result(r.status, r.result) == want
         assert r.phases == ph
+
+
+def test_serve_without_library_fails_requests():
+    """A worker that cannot open its context answers every request with the error
+    instead of leaving it waiting."""
+    reqs_f = small_requests(3, seed=7)
+    with Server(Options(all=1), library="/nonexistent/libsigma.so") as srv:
+        reqs = [srv.submit(f) for f in reqs_f]
+        for r in reqs:
+            assert r.wait(30)
+    assert all(r.status is not None and r.status < 0 and r.error for r in reqs)
