@@ -59,7 +59,11 @@ typedef struct {
     int32_t gc_freq;         /* "gcfreq"       = 2 (0: never compact inside the round) */
     /* GB300 extras (no counterpart in the reference) */
     int32_t dump_level;      /* 0: off, 1: per-phase summaries, 2: every stage */
-    int32_t reserved[7];
+    int32_t loop_limit;      /* rounds a device-side loop may run (election rounds, propagation
+                              * waves) before the round gives up with PF_ETIMEOUT; 0: the
+                              * default bound, variables + 2, which a correct round never reaches.
+                              * A small value exercises the give-up path without any wait. */
+    int32_t reserved[6];
 } pf_options;
 
 /* Per-round statistics (the reference's stage report, src/cpu/statistics.cpp:28-41,
@@ -150,13 +154,18 @@ pf_status pf_create_ot(uint32_t num_vars, const uint32_t* d_lits, const uint64_t
  * cannot take the device-wide synchronisation a cudaFree implies. Inputs and
  * outputs are the caller's device buffers, exactly as for pf_create_ot; the scan
  * scratch lives in a fixed 256 KiB array inside the library (held by every GPU
- * that loads the library until the process exits). Limit: num_vars <= 67,100,000
- * (2*num_vars+2 literal slots in 65,534 scan blocks of 2048); larger formulas get
- * PF_EINVAL. The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture. All calls share the one array: calls that overlap on the
- * GPU (other streams, other threads) race; serialise them. Calls no cudaMalloc,
- * cudaFree or other allocating routine, and creates no stream. */
+ * that loads the library until the process exits). Limit: num_vars <= 67,106,815
+ * (2*num_vars+2 literal slots in at most 65,534 scan blocks of 2048); larger
+ * formulas get PF_EINVAL before any GPU work. The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture. With lazy module loading (the
+ * CUDA default, CUDA_MODULE_LOADING=LAZY) that first call, and the first launch of
+ * each kernel it uses, also load code onto the device, which takes device memory:
+ * make one warm-up call (or set CUDA_MODULE_LOADING=EAGER) before the caller's pool
+ * reserves all of HBM; later calls take none. All calls share the one array:
+ * calls that overlap on the GPU (other streams, other threads) race; serialise
+ * them. Calls no cudaMalloc, cudaFree or other allocating routine (see
+ * pf_device_alloc_count), and creates no stream. */
 pf_status pf_create_ot_noalloc(uint32_t num_vars, const uint32_t* d_lits, const uint64_t* d_offsets,
                                uint64_t num_clauses, uint32_t* d_ot_off, uint32_t* d_ot_size, uint32_t* d_ot_refs,
                                void* stream);
@@ -201,6 +210,11 @@ pf_status pf_sigma_batch_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* o
 
 /* Device bytes held by the context. */
 pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes);
+
+/* Device allocations (cudaMalloc calls) this library has made in this process, over
+ * all contexts and calls. No counterpart in the reference: lets a caller that
+ * budgets device memory check that a call allocated nothing. */
+uint64_t pf_device_alloc_count(void);
 
 void pf_sigma_destroy(pf_sigma_ctx* ctx);
 

@@ -3,7 +3,9 @@
 # installer. Outputs go only to oracle/_ref/. Test infrastructure, never shipped.
 #
 #   make -f oracle/ref.mk REFDIR=/path/to/ParaFROST -j8
-REFDIR ?= /root/reference
+ifndef REFDIR
+$(error REFDIR=<path of the ParaFROST sources> is required)
+endif
 OUT    := oracle/_ref
 SRCDIR := $(REFDIR)/src/cpu
 CXX    ?= g++

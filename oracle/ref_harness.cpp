@@ -8,8 +8,11 @@
  * by reference code; the harness only adds snapshots between the steps and a
  * wall-clock timer around the phase loop (src/cpu/simplify.cpp:182-209).
  *
- * usage: sigma_ref <cnf.dimacs> <dump.bin> <level> [reference options...]
+ * usage: sigma_ref <cnf.dimacs> <dump.bin> <level> [--learnt-tail=N] [reference options...]
  *   level 0: input + final state + timing; 1: + per-phase summaries; 2: + every stage.
+ *   --learnt-tail=N: the last N parsed clauses become learnt clauses before the
+ *   round (an inprocessing call's input: awaken() extracts the original clauses,
+ *   then the learnt ones, src/cpu/simplify.cpp:147-148).
  */
 #include "solve.h"
 #include "dump.h"
@@ -37,6 +40,7 @@ static void on_exit_hook() {
 
 struct Harness : public ParaFROST {
     int level = 0;
+    uint32_t learnt_tail = 0;
     explicit Harness(const string& path) : ParaFROST(path) {}
 
     std::unordered_map<const SCLAUSE*, uint32_t> index_of() {
@@ -121,6 +125,17 @@ struct Harness : public ParaFROST {
             g_round_done = true;
             return;
         }
+        if (learnt_tail) {
+            // the last clauses of orgs move to the learnt list, marked learnt as the
+            // CDCL loop marks the clauses it learns (src/cpu/clause.h:151)
+            const uint32_t n = learnt_tail < orgs.size() ? learnt_tail : (uint32_t)orgs.size();
+            const uint32_t first = (uint32_t)orgs.size() - n;
+            for (uint32_t i = first; i < orgs.size(); i++) {
+                cm[orgs[i]].markLearnt();
+                learnts.push(orgs[i]);
+            }
+            orgs.resize(first);
+        }
         awaken();
         dump_cnf(0, sigdump::S_INPUT);
         dump_trail(0, sigdump::S_INPUT);
@@ -184,12 +199,17 @@ int main(int argc, char** argv) {
     std::vector<char*> args;
     args.push_back(argv[0]);
     args.push_back(argv[1]);
-    for (int i = 4; i < argc; i++) args.push_back(argv[i]);
+    uint32_t learnt_tail = 0;
+    for (int i = 4; i < argc; i++) {
+        if (!std::strncmp(argv[i], "--learnt-tail=", 14)) learnt_tail = (uint32_t)std::strtoul(argv[i] + 14, nullptr, 10);
+        else args.push_back(argv[i]);
+    }
     int n = (int)args.size();
     parseArguments(n, args.data());
     Harness* h = new Harness(argv[1]);
     pfrost = h;
     h->level = level;
+    h->learnt_tail = learnt_tail;
     h->round();
     return 0;
 }

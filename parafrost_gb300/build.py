@@ -21,7 +21,6 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libsigma_gb300.so")
 EMU = os.path.join(LIBDIR, "libsigma_emu.so")
 ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "libsigma_oracle.so")
-REF_DIR_DEFAULT = "/root/reference"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -82,22 +81,23 @@ def build_oracle(force: bool = False) -> str:
 
 
 def build_reference(refdir: str | None = None) -> str | None:
-    """Compile the reference CPU simplifier harness when the reference sources exist."""
-    refdir = refdir or os.environ.get("PARAFROST_REF", REF_DIR_DEFAULT)
-    if not os.path.isdir(os.path.join(refdir, "src", "cpu")):
+    """Compile the reference CPU simplifier harness when the reference sources exist:
+    their location is `refdir`, else the PARAFROST_REF environment variable."""
+    refdir = refdir or os.environ.get("PARAFROST_REF")
+    if not refdir or not os.path.isdir(os.path.join(refdir, "src", "cpu")):
         return None
     _run(["make", "-s", "-f", os.path.join("oracle", "ref.mk"), f"REFDIR={refdir}", f"-j{os.cpu_count() or 4}"])
     return os.path.join(ROOT, "oracle", "_ref", "sigma_ref")
 
 
-def build_all(with_cuda: bool = True) -> dict:
+def build_all(with_cuda: bool = True, refdir: str | None = None) -> dict:
     out = {}
     jobs = {"oracle": build_oracle, "emu": build_emu}
     if with_cuda:
         jobs["cuda"] = build_cuda
     with ThreadPoolExecutor(max_workers=len(jobs) + 1) as ex:
         futs = {k: ex.submit(f) for k, f in jobs.items()}
-        ref = ex.submit(build_reference)
+        ref = ex.submit(build_reference, refdir)
         for k, f in futs.items():
             out[k] = f.result()
         out["reference"] = ref.result()

@@ -17,6 +17,7 @@ struct UploadArgs {
     const u64* off;      // num_clauses + 1
     const uint8_t* learnt;  // may be null
     u64 base;            // literal offset of off[0]
+    u64 nlits;           // literals uploaded: every clause must lie in [base, base + nlits)
     // formula batches: nf formulas, formula f holds clauses [f_cls[f], f_cls[f+1])
     // and f_nv[f] variables from f_var[f]+1 on; its literals arrive in its own
     // numbering and are moved to the batch's (nf = 0: a single formula)
@@ -27,7 +28,11 @@ struct UploadArgs {
 };
 
 HD void k_upload_clause(const UploadArgs& a, u32 i) {
-    const u64 s = a.off[i] - a.base, e = a.off[i + 1] - a.base;
+    const u64 o0 = a.off[i], o1 = a.off[i + 1];
+    // offsets that go down, or leave the uploaded literals, are rejected before
+    // any literal is touched
+    if (o0 < a.base || o1 < o0 || o1 - a.base > a.nlits) { set_err(a.c, ERR_INPUT); return; }
+    const u64 s = o0 - a.base, e = o1 - a.base;
     u32* l = a.c.lits + s;
     const u32 n = (u32)(e - s);
     if (n == 0) { set_err(a.c, ERR_INPUT); return; }
@@ -91,7 +96,14 @@ struct CsrOtArgs {
     u32 D;
     u32* err;
 };
+// A clause whose offsets go down or leave [0, nlits) is an input error; neither
+// pass reads its literals.
+HD bool csr_clause_ok(const CsrOtArgs& a, u32 i) {
+    const u64 s = a.off[i], e = a.off[i + 1];
+    return s <= e && e <= a.nlits;
+}
 HD void k_hist_csr(const CsrOtArgs& a, u32 i) {
+    if (!csr_clause_ok(a, i)) { atom_or(a.err, ERR_INPUT); return; }
     for (u64 k = a.off[i]; k < a.off[i + 1]; k++) {
         const u32 lit = a.lits[k];
         if (lit < 2 || lit >= a.D) { atom_or(a.err, ERR_INPUT); continue; }
@@ -99,6 +111,7 @@ HD void k_hist_csr(const CsrOtArgs& a, u32 i) {
     }
 }
 HD void k_scatter_csr(const CsrOtArgs& a, u32 i) {
+    if (!csr_clause_ok(a, i)) return;
     for (u64 k = a.off[i]; k < a.off[i + 1]; k++) {
         const u32 lit = a.lits[k];
         if (lit < 2 || lit >= a.D) continue;

@@ -5,6 +5,7 @@
 
 #include "device.cuh"
 
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -30,6 +31,13 @@ inline void ck(cudaError_t e, const char* what) {
 #else
 typedef void* Stream;
 #endif
+
+// Device allocations made by the library in this process (every one goes through
+// Runtime::alloc); read by pf_device_alloc_count.
+inline std::atomic<unsigned long long>& device_alloc_count() {
+    static std::atomic<unsigned long long> n{0};
+    return n;
+}
 
 // Grid-stride launch of a functor f(i) for i in [0, n).
 #if SIGMA_CUDA
@@ -92,6 +100,7 @@ struct Runtime {
         p = std::malloc(bytes);
         if (!p) throw OomError("malloc failed");
 #endif
+        device_alloc_count().fetch_add(1, std::memory_order_relaxed);
         bytes_live += bytes;
         return p;
     }

@@ -615,7 +615,7 @@ struct pf_sigma_ctx {
             a.work = work.p;
             a.nwork = nullptr;
             a.cap_work = (u32)work.n;
-            PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, nvars + 2};
+            PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, loop_bound()};
             rt.zero(counters.p + 22, 5 * 4);  // [22..23] work counters, [24..25] barrier, [26] waves
             void* args[] = {&a, &w};
             rt.launches++;
@@ -632,7 +632,7 @@ struct pf_sigma_ctx {
 #else
         u32 guard = 0;
         while (prop_head < ntrail) {
-            if (++guard > nvars + 2) throw int(PF_ETIMEOUT);
+            if (++guard > loop_bound()) throw int(PF_ETIMEOUT);
             const u32 pend = ntrail - prop_head;
             PropArgs a;
             a.c = view();
@@ -718,7 +718,7 @@ struct pf_sigma_ctx {
         w.ctr = ctr;
         w.bar = ctr + 12;
         w.rounds = ctr + 14;
-        w.max_rounds = nvars + 2;
+        w.max_rounds = loop_bound();
         void* args[] = {&a, &w};
         kclock[K_MIS].start(rt);
         ck(cudaLaunchCooperativeKernel((const void*)mis_rounds_k, dim3(mis_rounds_grid()), dim3(256), args, 0,
@@ -734,7 +734,7 @@ struct pf_sigma_ctx {
             u32 n[4];
             rt.d2h(n, ctr + 4 * cur, 16);
             if (!n[0] && !n[1] && !n[2] && !n[3]) break;
-            if (++rounds > nvars + 2) throw int(PF_ETIMEOUT);
+            if (++rounds > loop_bound()) throw int(PF_ETIMEOUT);
             if (n[2]) rt.each(FMisPush{a, ins[cur].small}, n[2]);
             if (n[3]) rt.each(FMisPush{a, ins[cur].big}, n[3]);
             rt.zero(ctr + 4 * (cur ^ 1u), 16);
@@ -1203,6 +1203,9 @@ struct pf_sigma_ctx {
         const int times = phase + 1;
         if (opt.gc_freq > 0 && times > 1 && times != opt.phases && (times % opt.gc_freq) == 0) gc();
     }
+
+    // Rounds a device-side loop may run (election rounds, propagation waves).
+    u32 loop_bound() const { return opt.loop_limit > 0 ? (u32)opt.loop_limit : nvars + 2; }
 
     bool stop(i64 lr) const { return phase == opt.phases || (lr <= opt.ve_phase_min && phase > 2); }
 
@@ -1764,7 +1767,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         }
         DBuf<u64> dcls;
         DBuf<u32> dnv;
-        UploadArgs a{c.view(), off_ptr, learnt_ptr, off0, 0u, nullptr, nullptr, nullptr};
+        UploadArgs a{c.view(), off_ptr, learnt_ptr, off0, L, 0u, nullptr, nullptr, nullptr};
         if (batch) {
             const u32 nf = batch->nf;
             c.h_f_var = batch_var_offsets(nf, batch->num_vars);
@@ -1788,7 +1791,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
             c.f_phases.assign(nf, 0);
             c.res_mark.reserve(rt, c.resolved.n);
             rt.zero(c.res_mark.p, c.res_mark.n);
-            a = UploadArgs{c.view(), off_ptr, learnt_ptr, off0, nf, dcls.p, c.f_var.p, dnv.p};
+            a = UploadArgs{c.view(), off_ptr, learnt_ptr, parts ? 0ull : off0, L, nf, dcls.p, c.f_var.p, dnv.p};
         }
         rt.each(FUpload{a}, (u32)num_clauses);
         rt.sync();
@@ -2108,6 +2111,14 @@ pf_status pf_create_ot(uint32_t num_vars, const uint32_t* d_lits, const uint64_t
 // the device symbol; the device address comes from cudaGetSymbolAddress, looked
 // up once per device on that device's first call.
 constexpr u32 kNoallocWords = 1u << 16;  // 256 KiB
+// The scan over D = 2*num_vars+2 literal slots keeps ceil(D / 2048) + 1 block sums,
+// followed by one error word, so the largest accepted num_vars is 67,106,815.
+constexpr u64 kNoallocScanTile = 2048;
+constexpr u64 kNoallocMaxVars = (u64)(kNoallocWords - 2) * kNoallocScanTile / 2 - 1;
+static_assert(kNoallocMaxVars == 67106815ull, "no-allocation limit");
+#if SIGMA_CUDA
+static_assert(kScanTile == (int)kNoallocScanTile, "scan tile of the no-allocation limit");
+#endif
 #if SIGMA_CUDA
 static __device__ __align__(256) u32 g_noalloc_scratch[kNoallocWords];
 #else
@@ -2138,9 +2149,8 @@ pf_status pf_create_ot_noalloc(uint32_t num_vars, const uint32_t* d_lits, const 
                                void* stream) {
     if (!d_lits || !d_offsets || !d_ot_off || !d_ot_size || !d_ot_refs || !num_vars) return fail("null argument", PF_EINVAL);
     if (num_clauses >= 0xFFFFFF00ull) return fail("too many clauses", PF_EINVAL);
-    const u64 D = 2ull * ((u64)num_vars + 1);
-    if (num_vars >= (1u << 30) || scan_tmp_elems(D) + 1 > kNoallocWords)
-        return fail("pf_create_ot_noalloc: num_vars above 67,100,000 exceeds the fixed scratch", PF_EINVAL);
+    if (num_vars > kNoallocMaxVars)
+        return fail("pf_create_ot_noalloc: num_vars above 67,106,815 exceeds the fixed scratch", PF_EINVAL);
     return guarded([&]() -> pf_status {
         Runtime rt;  // no init(): this call creates no stream and allocates nothing
 #if SIGMA_CUDA
@@ -2156,6 +2166,8 @@ pf_status pf_create_ot_noalloc(uint32_t num_vars, const uint32_t* d_lits, const 
         return PF_OK;
     });
 }
+
+uint64_t pf_device_alloc_count(void) { return device_alloc_count().load(); }
 
 pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes) {
     if (!ctx || !bytes) return fail("null argument", PF_EINVAL);

@@ -94,6 +94,8 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     lib.pf_sigma_destroy.restype = None
     lib.pf_create_ot.argtypes = [_U32, _VP, _VP, _U64, _VP, _VP, _VP, _VP]
     lib.pf_create_ot.restype = ctypes.c_int
+    lib.pf_device_alloc_count.argtypes = []
+    lib.pf_device_alloc_count.restype = ctypes.c_uint64
     lib.pf_last_error.argtypes = []
     lib.pf_last_error.restype = ctypes.c_char_p
     return lib

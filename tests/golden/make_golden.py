@@ -43,6 +43,14 @@ CASES = [
     ("community_12k_s2", "community", dict(num_vars=4000, num_clauses=12000, communities=10, seed=2),
      dict(all=1, phases=3)),
     ("community_80k_s3", "community", dict(num_vars=20000, num_clauses=80000, communities=20, seed=3), dict(all=1)),
+    # inprocessing inputs: the last clauses enter the round as learnt clauses (after
+    # the original ones, the order awaken() extracts them in)
+    ("ksat3_10k_s5_learnt", "random_ksat", dict(num_vars=10_000, num_clauses=42_600, k=3, seed=5), dict(all=1),
+     8_000),
+    ("aig_30k_s6_learnt", "aig_tseitin", dict(num_inputs=2000, num_and=30000, num_xor=3000, seed=6), dict(all=1),
+     20_000),
+    ("community_12k_s7_learnt", "community", dict(num_vars=4000, num_clauses=12000, communities=10, seed=7),
+     dict(all=1, phases=3), 3_000),
 ]
 
 SMALL = 20_000  # keep full clause lists below this many output clauses
@@ -85,14 +93,17 @@ def main() -> None:
     if not orr.reference_available():
         raise SystemExit("compiled reference missing: run __graft_entry__.build() where the reference sources are")
     index = {}
-    for name, gen, kw, opt in CASES:
+    for name, gen, kw, opt, *tail in CASES:
+        learnt_tail = tail[0] if tail else 0
         nv, lits, off = getattr(cnfgen, gen)(**kw)
-        recs = orr.run_reference(nv, lits, off, Options(**opt), level=1)
+        recs = orr.run_reference(nv, lits, off, Options(**opt), level=1, learnt_tail=learnt_tail)
         s = summarize(recs)
         arrays = {k: v for k, v in s.items() if isinstance(v, np.ndarray)}
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
         meta = {k: v for k, v in s.items() if not isinstance(v, np.ndarray) and v is not None}
         meta.update(generator=gen, kwargs=kw, options=opt, input_hash=digest(lits, off), num_vars=nv)
+        if learnt_tail:
+            meta["learnt_tail"] = learnt_tail
         index[name] = meta
         print(name, meta["status"], meta.get("num_clauses"), meta["pv_counts"])
     with open(os.path.join(HERE, "index.json"), "w") as f:

@@ -22,6 +22,17 @@ def load(name: str):
     return meta, arrays, (nv, lits, off), Options(**meta["options"])
 
 
+def learnt_mask(meta: dict, off: np.ndarray):
+    """Learnt flag per clause of a case (None when every clause is original): the
+    last learnt_tail clauses are learnt."""
+    n = int(meta.get("learnt_tail", 0))
+    if not n:
+        return None
+    m = np.zeros(off.size - 1, dtype=np.uint8)
+    m[m.size - n:] = 1
+    return m
+
+
 def check(meta: dict, arrays: dict, recs: list) -> list:
     """Compare a round dump (level >= 1) against a golden case; returns mismatches."""
     import sys

@@ -97,13 +97,15 @@ def reference_available() -> bool:
     return os.path.exists(REF_BIN)
 
 
-def run_reference(num_vars, lits, offsets, opts: Options | None = None, level: int = 2):
-    """Run the compiled reference round through its own DIMACS parser; returns records."""
+def run_reference(num_vars, lits, offsets, opts: Options | None = None, level: int = 2, learnt_tail: int = 0):
+    """Run the compiled reference round through its own DIMACS parser; returns records.
+    With learnt_tail, the last learnt_tail clauses enter the round as learnt clauses."""
     opts = opts or Options(all=1)
     with tempfile.TemporaryDirectory() as td:
         cnf = os.path.join(td, "f.cnf")
         dump = os.path.join(td, "ref.dump")
         cnfgen.to_dimacs(cnf, num_vars, lits, offsets)
-        args = [REF_BIN, cnf, dump, str(level)] + opts.reference_flags()
+        args = [REF_BIN, cnf, dump, str(level)] + ([f"--learnt-tail={learnt_tail}"] if learnt_tail else [])
+        args += opts.reference_flags()
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
         return rounddump.read(dump)

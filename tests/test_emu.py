@@ -13,10 +13,10 @@ from parafrost_gb300.options import Options
 from parafrost_gb300.sigma import Simplifier
 
 
-def run_lib(library, nv, lits, off, opts, level=2):
+def run_lib(library, nv, lits, off, opts, level=2, learnt=None):
     op = Options(**{**opts.__dict__, "dump_level": level})
     with Simplifier(op, library=library) as s:
-        s.awaken(nv, lits, off)
+        s.awaken(nv, lits, off, learnt)
         stats = s.sigmify()
         with tempfile.TemporaryDirectory() as td:
             p = os.path.join(td, "d.bin")
@@ -31,7 +31,7 @@ def test_emu_golden(built, name):
     meta, arrays, (nv, lits, off), opts = gc.load(name)
     if meta.get("num_clauses", 0) > 60000 or nv > 50000:
         pytest.skip("large case: GPU test only")
-    stats, recs, _ = run_lib(build.EMU, nv, lits, off, opts, level=1)
+    stats, recs, _ = run_lib(build.EMU, nv, lits, off, opts, level=1, learnt=gc.learnt_mask(meta, off))
     assert stats.status == meta["status"]
     assert gc.check(meta, arrays, recs) == []
 

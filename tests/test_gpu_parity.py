@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("name", sorted(gc.index()))
 def test_gpu_golden(cuda_lib, name):
     meta, arrays, (nv, lits, off), opts = gc.load(name)
-    stats, recs, _ = run_lib(cuda_lib, nv, lits, off, opts, level=1)
+    stats, recs, _ = run_lib(cuda_lib, nv, lits, off, opts, level=1, learnt=gc.learnt_mask(meta, off))
     assert stats.status == meta["status"]
     assert gc.check(meta, arrays, recs) == []
 

@@ -12,7 +12,7 @@ from make_golden import digest
 def test_oracle_matches_reference_golden(built, name):
     meta, arrays, (nv, lits, off), opts = gc.load(name)
     assert digest(lits, off) == meta["input_hash"], "generator output changed"
-    st, recs, _ = orr.run_oracle(nv, lits, off, opts, level=1)
+    st, recs, _ = orr.run_oracle(nv, lits, off, opts, level=1, learnt=gc.learnt_mask(meta, off))
     assert st == meta["status"]
     assert gc.check(meta, arrays, recs) == []
 
