@@ -1,19 +1,24 @@
 """Benchmark: one sigmify round (ParaFROST's GPU inprocessing round) per step.
 
-Workload (default): Tseitin encoding of a seeded random AIG with 2M AND and
-200k XOR gates over 50k inputs (6.8M clauses, 16.4M literals, 2.25M variables),
-synthetic, generated in-process. A step = device-side awaken (copy of the
-resident input + literal sort + signatures) + one full round with the
-reference's default phase settings and -all (VE, SUB, BCE, ERE). Metric unit:
-input clauses simplified per second (whole job; N GPUs run N independent
-replicas: the round does not shard, so there is no collective).
+Workload (default, community-20m): a seeded community-attachment CNF with 20M
+variables and 80M clauses (200 communities, modularity 0.8, clause length
+geometric with mean 3.5 clipped to [2, 64], power-law variable frequency with
+exponent 2.5; 280M literals), synthetic, generated in-process. aig-2.2m is the
+Tseitin encoding of a seeded random AIG with 2M AND and 200k XOR gates over 50k
+inputs (6.8M clauses). A step = device-side awaken (copy of the resident input +
+literal sort + signatures) + one full round with the reference's default phase
+settings and -all (VE, SUB, BCE, ERE). Metric unit: input clauses simplified per
+second (whole job; N GPUs run N independent replicas: the round does not shard,
+so there is no collective). The line also carries every phase's live size,
+elected variables, algorithmic bytes and device time.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload W]
 
 The reference arm times the reference's CPU simplifier on the host cores: the
 compiled reference (oracle/_ref) when present, else the oracle port of it
-(oracle/_build), on a bounded sample of the same workload (a 1/8-size AIG of the
-same generator), in the same unit.
+(oracle/_build), in the same unit: on the full AIG workload, and on a 1/10-size
+formula of the same generator for the community workload (a full 80M-clause
+round takes about 1.5 minutes on one core, too long for every step).
 """
 from __future__ import annotations
 
@@ -34,7 +39,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 WORKLOADS = {
     "aig-2.2m": dict(gen="aig_tseitin", kw=dict(num_inputs=50_000, num_and=2_000_000, num_xor=200_000, seed=1),
-                     sample_kw=dict(num_inputs=6_250, num_and=250_000, num_xor=25_000, seed=1)),
+                     sample_kw=dict(num_inputs=50_000, num_and=2_000_000, num_xor=200_000, seed=1)),
     "community-20m": dict(gen="community", kw=dict(seed=1),
                           sample_kw=dict(num_vars=2_000_000, num_clauses=8_000_000, seed=1)),
     "ksat3-10k": dict(gen="random_ksat", kw=dict(num_vars=10_000, num_clauses=42_600, k=3, seed=1),
@@ -196,11 +201,16 @@ def run_reference(args) -> dict:
         times.append(s)
     tot = float(np.sum(times))
     value = ncls * args.steps / tot
-    sample = f"{WORKLOADS[args.workload]['sample_kw']} ({ncls} clauses), one full round per step, 1 thread"
+    spec = WORKLOADS[args.workload]
+    full = spec["sample_kw"] == spec["kw"]
+    sample = (f"{spec['sample_kw']} ({ncls} clauses, {'the full workload' if full else 'a smaller formula of the same generator'}),"
+              " one full round per step, 1 thread (the reference simplifier has no threads)")
     return {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic", "config": {"workload": args.workload, "sample": True},
+            "data": "synthetic",
+            "config": {"workload": args.workload, "sample": not full, "clauses": int(ncls), "literals": int(lits.size),
+                       "vars": int(nv), "options": "-all, phases=5"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -243,6 +253,16 @@ def profiled_utilisation(kernel: str, workload: str):
         return None
     return {"sm_throughput_pct": float(kv["sm_pct"]), "dram_throughput_pct": float(kv["dram_pct"]),
             "launch": kv.get("measured_launch"), "source": "profiles/dram_traffic.txt (ncu --set full)"}
+
+
+def phase_rows(stats, peak: float) -> list:
+    """Every phase of a round: live clauses and literals entering it, variables
+    elected, algorithmic bytes, device time, and their ratio against the peak."""
+    rows = []
+    for r in stats.as_dict()["phases"]:
+        gbs = r["bytes"] / (r["ms"] / 1e3) / 1e9 if r["ms"] > 0 else None
+        rows.append({**r, "gbs": gbs, "frac": gbs / peak if gbs else None})
+    return rows
 
 
 def flush_l2(buf):
@@ -381,13 +401,15 @@ def run_ours(args) -> dict:
            "kernels": kern,
            "round_roofline": {"achieved": round_gbs, "frac": round_gbs / peak,
                               "scope": "whole round: algorithmic bytes / round device time"},
+           "phases": phase_rows(last, peak),
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(lits.nbytes + off.nbytes),
                    "d2h_bytes_per_step": int(d2h),
                    "ms": {"upload": parts_ms[0], "round": parts_ms[1], "download": parts_ms[2]}},
            "gpu_launches": launches, "clocks": clk}
     s.close()
     if rank == 0 and not args.no_cpu_baseline:
-        snv, sl, so = make_workload(args.workload, sample=True)
+        spec = WORKLOADS[args.workload]
+        snv, sl, so = (nv, lits, off) if spec["sample_kw"] == spec["kw"] else make_workload(args.workload, sample=True)
         secs, kind = cpu_round_seconds(snv, sl, so)
         out["cpu_baseline"] = {"value": (so.size - 1) / secs, "unit": UNIT, "cores": 1, "kind": kind,
                                "sample": f"{WORKLOADS[args.workload]['sample_kw']} ({so.size - 1} clauses), one round"}
@@ -603,7 +625,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="aig-2.2m")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="community-20m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-sequential", action="store_true", help="batched workload: skip the one-by-one comparison")

@@ -87,6 +87,14 @@ typedef struct {
     double ms_kernel[4];        /* device time summed over the round's launches */
     uint64_t bytes_kernel[4];   /* algorithmic bytes those launches processed */
     uint32_t launches_kernel[4];
+    /* Per phase p < 8 of the round (a batch: the batch's shared phase p): live
+     * clauses and literals entering it, variables elected in it, the algorithmic
+     * bytes and device time of its stages (the closing propagation, count and
+     * compaction after the last phase are in neither). */
+    uint32_t phase_elected[8];
+    uint64_t phase_clauses[8], phase_literals[8];
+    uint64_t phase_bytes[8];
+    double phase_ms[8];
 } pf_round_stats;
 
 typedef struct pf_sigma_ctx pf_sigma_ctx;

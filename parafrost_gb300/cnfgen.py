@@ -321,17 +321,27 @@ def community(num_vars: int = 20_000_000, num_clauses: int = 80_000_000, communi
         rank = np.searchsorted(cdf, st.unit(total), side="right")
         rank = np.minimum(rank, per - 1)
         var = perm[lit_comm * per + rank].astype(np.int64)
-        # redraw repeated variables inside a clause
+        # redraw repeated variables inside a clause; after the first pass only the
+        # clauses that had a repeat can have one, so later passes look at those alone
+        # (their positions keep the same relative order, so the redraws are the same)
         starts = np.concatenate([[0], np.cumsum(k)[:-1]])
+        idx = None
         while True:
-            key = owner * np.int64(num_vars + 1) + var
+            o = owner if idx is None else owner[idx]
+            key = o * np.int64(num_vars + 1) + (var if idx is None else var[idx])
             order = np.argsort(key, kind="stable")
             sk = key[order]
             dup = order[1:][sk[1:] == sk[:-1]]
+            if idx is not None:
+                dup = idx[dup]
             if dup.size == 0:
                 break
             rr = np.minimum(np.searchsorted(cdf, st.unit(dup.size), side="right"), per - 1)
             var[dup] = perm[lit_comm[dup] * per + rr]
+            own = np.unique(owner[dup])
+            lens = k[own]
+            first = np.cumsum(lens) - lens
+            idx = np.repeat(starts[own] - first, lens) + np.arange(int(lens.sum()), dtype=np.int64)
         sign = st.below(2, total)
         if planted is not None:
             sign = _plant(st, planted, var, sign, owner, n)
@@ -367,13 +377,15 @@ def aig_model(num_inputs: int = 50_000, num_and: int = 2_000_000, num_xor: int =
     return np.array(vl, dtype=np.uint8)
 
 
-def batch_ksat(num_formulas: int = 4096, cmin: int = 1_000, cmax: int = 200_000, seed: int = 1):
-    """Batched workload: clause counts log-uniform in [cmin, cmax], ratio U[3.0, 4.5], k in 2..5."""
+def batch_ksat(num_formulas: int = 4096, cmin: int = 1_000, cmax: int = 200_000, seed: int = 1,
+               indices=None):
+    """Batched workload: clause counts log-uniform in [cmin, cmax], ratio U[3.0, 4.5], k in 2..5.
+    ``indices`` picks formulas of the batch (each is generated on its own seed)."""
     st = Stream(seed, 5)
     u = st.unit(num_formulas)
     counts = np.exp(np.log(cmin) + u * (np.log(cmax) - np.log(cmin))).astype(np.int64)
     ratios = 3.0 + 1.5 * st.unit(num_formulas)
-    for i in range(num_formulas):
+    for i in (range(num_formulas) if indices is None else indices):
         yield random_mixed_ksat(int(counts[i]), float(ratios[i]), seed=seed * 1_000_003 + i)
 
 

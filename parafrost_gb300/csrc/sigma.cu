@@ -1209,6 +1209,29 @@ struct pf_sigma_ctx {
 
     bool stop(i64 lr) const { return phase == opt.phases || (lr <= opt.ve_phase_min && phase > 2); }
 
+    // Per-phase figures of the round (pf_round_stats phase_*): opened at the top of
+    // a phase with the live counts entering it, closed where the phase ends.
+    u64 ph_bytes0 = 0;
+    double ph_ms0 = 0;
+    double stage_ms_sum() const {
+        double t = 0;
+        for (double x : st.ms_stage) t += x;
+        return t;
+    }
+    void phase_open(i64 cls, i64 lits) {
+        if (phase >= 8) return;
+        st.phase_clauses[phase] = (u64)cls;
+        st.phase_literals[phase] = (u64)lits;
+        ph_bytes0 = alg_bytes;
+        ph_ms0 = stage_ms_sum();
+    }
+    void phase_close() {
+        if (phase >= 8) return;
+        st.phase_elected[phase] = npvs;
+        st.phase_bytes[phase] = alg_bytes - ph_bytes0;
+        st.phase_ms[phase] = stage_ms_sum() - ph_ms0;
+    }
+
     double timed(int stage, void (pf_sigma_ctx::*fn)()) {
         tm.start(rt);
         (this->*fn)();
@@ -1226,6 +1249,7 @@ struct pf_sigma_ctx {
         st.clauses_before = (u64)n_cls_after;
         st.literals_before = (u64)n_lits_after;
         while (litsbefore) {
+            phase_open(n_cls_after, litsbefore);
             timed(ST_GC, &pf_sigma_ctx::resize_cnf);
             timed(ST_OT, &pf_sigma_ctx::create_ot);
             timed(ST_PROP, &pf_sigma_ctx::prop);
@@ -1236,7 +1260,10 @@ struct pf_sigma_ctx {
             tm.start(rt);
             const bool go = lcve();
             st.ms_stage[ST_LCVE] += tm.stop(rt);
-            if (!go) break;
+            if (!go) {
+                phase_close();
+                break;
+            }
             timed(ST_SORT, &pf_sigma_ctx::sort_ot);
             if (opt.dump_level >= 2) dump_pvlists(phase);
             const u64 W = pv_bytes();
@@ -1246,6 +1273,7 @@ struct pf_sigma_ctx {
                 timed(ST_ERE, &pf_sigma_ctx::ere);
                 alg_bytes += W;
                 dump_stage(phase, 7);
+                phase_close();
                 break;
             }
             timed(ST_SUB, &pf_sigma_ctx::sub);
@@ -1256,6 +1284,7 @@ struct pf_sigma_ctx {
             dump_stage(phase, 6);
             alg_bytes += 4ull * W;
             timed(ST_COUNT, &pf_sigma_ctx::count_all);
+            phase_close();
             if (opt.dump_level >= 1) {
                 rec(10, phase, 6, {(u32)n_cls_after, (u32)n_lits_after});
                 dump_elim(phase, 6);
@@ -1479,6 +1508,7 @@ struct pf_sigma_ctx {
             bool any = false;
             for (u32 f = 0; f < nf; f++) any |= !done[f];
             if (!any) break;
+            phase_open(n_cls_after, n_lits_after);
             timed(ST_GC, &pf_sigma_ctx::resize_cnf);
             timed(ST_OT, &pf_sigma_ctx::create_ot);
             timed(ST_PROP, &pf_sigma_ctx::prop);
@@ -1502,7 +1532,10 @@ struct pf_sigma_ctx {
             }
             partition_pvs(group);
             st.ms_stage[ST_LCVE] += tm.stop(rt);
-            if (!going) continue;
+            if (!going) {
+                phase_close();
+                continue;
+            }
             timed(ST_SORT, &pf_sigma_ctx::sort_ot);
             const u64 W = pv_bytes();
             phase_ws = W;
@@ -1524,6 +1557,7 @@ struct pf_sigma_ctx {
             }
             alg_bytes += 4ull * W;
             timed(ST_COUNT, &pf_sigma_ctx::count_formulas);
+            phase_close();
             mark_unsat(done);
             for (u32 f = 0; f < nf; f++) {
                 if (done[f]) continue;

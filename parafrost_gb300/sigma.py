@@ -47,14 +47,24 @@ class RoundStats(ctypes.Structure):
                 ("ms_stage", ctypes.c_double * 12), ("algorithmic_bytes", ctypes.c_uint64),
                 ("kernel_launches", ctypes.c_uint32), ("mis_rounds", ctypes.c_uint32),
                 ("reserved", ctypes.c_uint32 * 2), ("ms_kernel", ctypes.c_double * 4),
-                ("bytes_kernel", ctypes.c_uint64 * 4), ("launches_kernel", ctypes.c_uint32 * 4)]
+                ("bytes_kernel", ctypes.c_uint64 * 4), ("launches_kernel", ctypes.c_uint32 * 4),
+                ("phase_elected", ctypes.c_uint32 * 8), ("phase_clauses", ctypes.c_uint64 * 8),
+                ("phase_literals", ctypes.c_uint64 * 8), ("phase_bytes", ctypes.c_uint64 * 8),
+                ("phase_ms", ctypes.c_double * 8)]
+
+    PHASE_FIELDS = ("phase_elected", "phase_clauses", "phase_literals", "phase_bytes", "phase_ms")
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_
-             if f not in ("ms_stage", "reserved", "ms_kernel", "bytes_kernel", "launches_kernel")}
+             if f not in ("ms_stage", "reserved", "ms_kernel", "bytes_kernel", "launches_kernel")
+             and f not in self.PHASE_FIELDS}
         d["ms_stage"] = {s: self.ms_stage[i] for i, s in enumerate(STAGES)}
         d["kernels"] = {k: {"ms": self.ms_kernel[i], "bytes": int(self.bytes_kernel[i]),
                             "launches": int(self.launches_kernel[i])} for i, k in enumerate(HOT_KERNELS)}
+        d["phases"] = [{"phase": p, "clauses": int(self.phase_clauses[p]), "literals": int(self.phase_literals[p]),
+                        "elected": int(self.phase_elected[p]), "bytes": int(self.phase_bytes[p]),
+                        "ms": self.phase_ms[p]} for p in range(min(int(self.phases_run) + 1, 8))
+                       if self.phase_ms[p] > 0 or self.phase_clauses[p] > 0]
         return d
 
 

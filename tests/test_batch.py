@@ -83,6 +83,14 @@ def test_batch_gpu(cuda_lib, built, opt):
 @pytest.mark.gpu
 def test_batch_gpu_many(cuda_lib):
     """64 random k-SAT formulas with 1k-20k clauses (the batched workload's
-    generator at a smaller size) against their own rounds."""
+    generator at a smaller size) against their own rounds and the oracle."""
     forms = list(cnfgen.batch_ksat(num_formulas=64, cmin=1_000, cmax=20_000, seed=9))
-    check_batch(cuda_lib, forms, Options(all=1), oracle=False)
+    check_batch(cuda_lib, forms, Options(all=1), oracle=True)
+
+
+@pytest.mark.gpu
+def test_batch_gpu_workload_slice(cuda_lib):
+    """64 formulas of the batched benchmark's own generator and sizes (1k-200k
+    clauses, k mixed 2-5), every one against the oracle."""
+    forms = list(cnfgen.batch_ksat(num_formulas=4096, cmin=1_000, cmax=200_000, seed=1, indices=range(0, 4096, 64)))
+    check_batch(cuda_lib, forms, Options(all=1), oracle=True)
