@@ -15,7 +15,7 @@ CXXFLAGS := -std=c++17 -DNDEBUG -O3 -fPIC -w -include cstdint -include cstddef -
 SRCS := $(filter-out $(SRCDIR)/main.cpp,$(sort $(wildcard $(SRCDIR)/*.cpp)))
 OBJS := $(patsubst $(SRCDIR)/%.cpp,$(OUT)/obj/%.o,$(SRCS))
 
-all: $(OUT)/libpfref.a $(OUT)/sigma_ref
+all: $(OUT)/libpfref.a $(OUT)/sigma_ref $(OUT)/parafrost
 
 $(OUT)/obj/%.o: $(SRCDIR)/%.cpp
 	@mkdir -p $(OUT)/obj
@@ -25,6 +25,10 @@ $(OUT)/libpfref.a: $(OBJS)
 	ar rcs $@ $^
 
 $(OUT)/sigma_ref: oracle/ref_harness.cpp $(OUT)/libpfref.a
+	$(CXX) $(CXXFLAGS) -I$(SRCDIR) $< -o $@ $(OUT)/libpfref.a
+
+# the reference solver's own command line (CDCL search; equisatisfiability checks)
+$(OUT)/parafrost: $(SRCDIR)/main.cpp $(OUT)/libpfref.a
 	$(CXX) $(CXXFLAGS) -I$(SRCDIR) $< -o $@ $(OUT)/libpfref.a
 
 .PHONY: all

@@ -155,7 +155,10 @@ struct Round {
     }
 
     // ---------------------------------------------------------------- extract / OT
-    // ParaFROST::extract (src/cpu/simplify.cpp:95-113).
+    // ParaFROST::extract (src/cpu/simplify.cpp:95-113). A one-literal clause is a unit
+    // the reference's parser puts on the trail (src/cpu/dimacs.cpp:153-159): it is
+    // enqueued (the opposite literal already there: UNSAT) and kept as a deleted slot.
+    bool input_unsat = false;
     void extract(const u32* lits, const uint64_t* off, uint64_t n, const uint8_t* learnt) {
         arena.reserve(n + n / 4);
         scnf.reserve(n + n / 4);
@@ -165,11 +168,35 @@ struct Round {
             c.lits.assign(lits + off[i], lits + off[i + 1]);
             c.calcSig();
             std::sort(c.lits.begin(), c.lits.end());
-            nLiterals += c.size();
-            nClauses++;
+            if (c.size() == 1) {
+                const u32 u = c.lits[0];
+                if (unassigned(u)) enqueueUnit(u);
+                else if (value[u] == 0) input_unsat = true;
+                c.st = ST_DELETED;
+            } else {
+                nLiterals += c.size();
+                nClauses++;
+            }
             scnf.push_back((u32)arena.size());
             arena.push_back(std::move(c));
         }
+    }
+
+    // rootify() + shrinkTop() at the start of sigmifying() (src/cpu/simplify.cpp:163-164,
+    // shrink.cpp:152-216): the input units propagated at the root, satisfied clauses
+    // dropped and false literals removed before the first occurrence table. Here the
+    // same fixpoint by prop() over a table of the input, then shrinkSimp(). Returns
+    // false when no clause is left (the reference then skips the round).
+    bool rootUnits() {
+        if (input_unsat) throw Unsat();
+        if (propagated >= trail.size()) return true;
+        createOT();
+        prop();
+        shrinkSimp();
+        countAll();
+        nClauses = n_cls_after;
+        nLiterals = n_lits_after;
+        return !scnf.empty();
     }
 
     // ParaFROST::createOT (simplify.cpp:35-56).
@@ -1145,7 +1172,9 @@ int oracle_sigmify(const pf_options* opts, uint32_t num_vars, const uint32_t* li
         R->dump_trail(0, sigdump::S_INPUT);
         auto t0 = std::chrono::steady_clock::now();
         try {
-            R->run();
+            // with nothing left after the root propagation the reference skips the
+            // round; its state (units, no clause) is the final state dumped here
+            if (R->rootUnits()) R->run();
         } catch (Unsat&) {
             status = 1;
         }

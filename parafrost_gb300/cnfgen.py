@@ -377,6 +377,32 @@ def aig_model(num_inputs: int = 50_000, num_and: int = 2_000_000, num_xor: int =
     return np.array(vl, dtype=np.uint8)
 
 
+def with_units(num_vars: int, lits: np.ndarray, offsets: np.ndarray, count: int, seed: int = 1,
+               model: np.ndarray | None = None) -> tuple:
+    """The formula with ``count`` one-literal clauses appended (seeded random
+    variables, repeats allowed; random signs, or the signs that make them true
+    under ``model``, uint8 per variable): the root-level units an incremental or
+    BMC front end passes along with its clauses."""
+    st = Stream(seed, 11)
+    var = 1 + st.below(num_vars, count)
+    sign = st.below(2, count) if model is None else (1 - np.asarray(model, dtype=np.int64)[var])
+    units = ((var << 1) | sign).astype(np.uint32)
+    off = np.concatenate([offsets, offsets[-1] + 1 + np.arange(count, dtype=np.uint64)]).astype(np.uint64)
+    return num_vars, np.concatenate([lits, units]), off
+
+
+def with_units_of(gen: str, count: int, unit_seed: int = 1, **kw) -> tuple:
+    """``with_units`` over the formula ``gen(**kw)`` of this module, with units true
+    under the formula's known model (AIG inputs evaluated, or the community
+    formula's planted assignment)."""
+    model = None
+    if gen == "aig_tseitin":
+        model = aig_model(**kw)
+    elif gen == "community":
+        model = community_planted(kw["num_vars"], kw.get("seed", 1))
+    return with_units(*globals()[gen](**kw), count=count, seed=unit_seed, model=model)
+
+
 def batch_ksat(num_formulas: int = 4096, cmin: int = 1_000, cmax: int = 200_000, seed: int = 1,
                indices=None):
     """Batched workload: clause counts log-uniform in [cmin, cmax], ratio U[3.0, 4.5], k in 2..5.

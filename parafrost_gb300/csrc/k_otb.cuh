@@ -1,0 +1,211 @@
+// Occurrence-table build by literal buckets (createOT, src/cpu/simplify.cpp:35-56;
+// GPU reference: histogram.cu:34-52, memory.cu:271-312, create_ot_k kernels.cu:81-96).
+//
+// The literal slots are cut into buckets of 2^shift consecutive slots. No pass
+// issues one device-memory atomic per occurrence, and no pass writes outside the
+// range of the bucket it works on:
+//   pass 0 (ot_bucket_count_k): every occurrence (a literal of a live clause) adds
+//     one to its bucket in a per-block shared histogram; one atomic per bucket per
+//     block at the end. An exclusive scan of the bucket counts gives every bucket
+//     its range of the table (all its literals' lists, side by side).
+//   pass 1 (ot_bucket_fill_k): per tile of clauses, the same histogram in shared
+//     memory, one reservation per non-empty bucket, then each occurrence (literal,
+//     clause id) goes to its bucket's reserved run (two plain arrays).
+//   pass 2 (ot_bucket_lists_k): one block per bucket: per-slot counts in shared
+//     memory, a block scan gives the list sizes and starts of the bucket's slots,
+//     then every occurrence lands in its list inside the bucket's range.
+// Clause headers and literals are read by whole warps, consecutive lanes on
+// consecutive literals. Equal keys inside a warp are combined (__match_any_sync)
+// before their shared-memory atomic, so a literal with millions of occurrences
+// costs one atomic per warp step. The order inside one list is unspecified, as for
+// the atomic build: the elected lists are sorted into the reference's order later.
+#pragma once
+
+#include "cnf.cuh"
+
+namespace sigma {
+
+#if SIGMA_CUDA
+
+constexpr u32 OTB_TILE = 4096;      // clauses per block tile in passes 0 and 1
+constexpr u32 OTB_MAX_BUCKETS = 4096;
+constexpr u32 OTB_MAX_SHIFT = 15;   // 32,768 slots: 128 KiB of shared counters in pass 2
+constexpr u32 OTB_LIST_THREADS = 512;
+constexpr unsigned OTB_FULL = 0xffffffffu;
+
+struct OtbArgs {
+    Ctx c;
+    u32 shift;        // bucket of literal l: l >> shift
+    u32 nb;           // buckets
+    u32* count;       // nb: occurrences per bucket (pass 0)
+    u32* cursor;      // nb: next free position of every bucket (pass 1; starts at base)
+    const u32* base;  // nb + 1: first position of every bucket, base[nb] = occurrences
+    u32* tlit;        // occurrences grouped by bucket: literal
+    u32* tcid;        //   and clause id
+};
+
+// The literals of the live clauses id0 .. id0+n-1 (n <= 32), walked by one warp with
+// consecutive lanes on consecutive literals (clauses are mostly adjacent in the
+// literal array, so the loads coalesce). f(valid, literal, clause id) is called by
+// every lane of the warp in every step, valid false past the end.
+template <class F>
+DEV void warp_clause_literals(const Ctx& c, u32 id0, u32 n, F&& f) {
+    const u32 lane = threadIdx.x & 31u;
+    u32 start = 0, sz = 0;
+    if (lane < n) {
+        const Hdr h = hdr_ro(&c.hdr[id0 + lane]);
+        if (!h_deleted(h.flags)) {
+            start = h.start;
+            sz = h.size;
+        }
+    }
+    u32 incl = sz;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 t = __shfl_up_sync(OTB_FULL, incl, o);
+        if ((int)lane >= o) incl += t;
+    }
+    const u32 excl = incl - sz;
+    const u32 total = __shfl_sync(OTB_FULL, incl, 31);
+    for (u32 base = 0; base < total; base += 32) {
+        const u32 j = base + lane;
+        // owner: the first lane k whose inclusive end is past j
+        u32 k = 0;
+#pragma unroll
+        for (u32 step = 16; step; step >>= 1) {
+            const u32 v = __shfl_sync(OTB_FULL, incl, k + step - 1);
+            if (v <= j) k += step;
+        }
+        const u32 st = __shfl_sync(OTB_FULL, start, k & 31u), ex = __shfl_sync(OTB_FULL, excl, k & 31u);
+        const bool valid = j < total;
+        const u32 lit = valid ? __ldg(&c.lits[st + (j - ex)]) : 0u;
+        f(valid, lit, id0 + k);
+    }
+}
+
+// Adds 1 for key to counter ctr[key] in shared memory from every valid lane; lanes
+// with the same key add together. Returns, for each valid lane, its rank among the
+// lanes of its key plus the counter's value before the add.
+DEV u32 warp_smem_rank(u32* ctr, bool valid, u32 key) {
+    const u32 lane = threadIdx.x & 31u;
+    const u32 peers = __match_any_sync(OTB_FULL, valid ? key : 0xffffffffu);
+    const u32 leader = __ffs(peers) - 1;
+    u32 old = 0;
+    if (valid && lane == leader) old = atomicAdd(&ctr[key], (u32)__popc(peers));
+    old = __shfl_sync(OTB_FULL, old, leader);
+    return old + (u32)__popc(peers & ((1u << lane) - 1u));
+}
+
+// Pass 0: occurrences per bucket.
+__global__ void __launch_bounds__(256) ot_bucket_count_k(OtbArgs a) {
+    extern __shared__ u32 otb_hist[];
+    for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) otb_hist[b] = 0;
+    __syncthreads();
+    const u32 warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const u32 ngroups = (a.c.ncls + 31u) / 32u;
+    for (u32 g = blockIdx.x * nw + warp; g < ngroups; g += gridDim.x * nw) {
+        const u32 id0 = g * 32u;
+        const u32 n = a.c.ncls - id0 < 32u ? a.c.ncls - id0 : 32u;
+        warp_clause_literals(a.c, id0, n, [&](bool valid, u32 lit, u32) {
+            warp_smem_rank(otb_hist, valid, lit >> a.shift);
+        });
+    }
+    __syncthreads();
+    for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x)
+        if (otb_hist[b]) atomicAdd(&a.count[b], otb_hist[b]);
+}
+
+// Pass 1: occurrences grouped by bucket, one reservation per bucket per tile.
+__global__ void __launch_bounds__(256) ot_bucket_fill_k(OtbArgs a) {
+    extern __shared__ u32 otb_sm[];
+    u32* hist = otb_sm;        // nb: tile counts, then ranks inside the tile
+    u32* run = otb_sm + a.nb;  // nb: the tile's reserved start in every bucket
+    const u32 warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const u32 ntiles = (a.c.ncls + OTB_TILE - 1u) / OTB_TILE;
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) hist[b] = 0;
+        __syncthreads();
+        const u32 c0 = t * OTB_TILE, c1 = a.c.ncls - c0 < OTB_TILE ? a.c.ncls : c0 + OTB_TILE;
+        for (u32 g = c0 + warp * 32u; g < c1; g += nw * 32u)
+            warp_clause_literals(a.c, g, c1 - g < 32u ? c1 - g : 32u, [&](bool valid, u32 lit, u32) {
+                warp_smem_rank(hist, valid, lit >> a.shift);
+            });
+        __syncthreads();
+        for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) {
+            const u32 n = hist[b];
+            run[b] = n ? atomicAdd(&a.cursor[b], n) : 0u;
+            hist[b] = 0;
+        }
+        __syncthreads();
+        for (u32 g = c0 + warp * 32u; g < c1; g += nw * 32u)
+            warp_clause_literals(a.c, g, c1 - g < 32u ? c1 - g : 32u, [&](bool valid, u32 lit, u32 cid) {
+                const u32 b = lit >> a.shift;
+                const u32 r = warp_smem_rank(hist, valid, b);
+                if (valid) {
+                    const u32 pos = run[b] + r;
+                    a.tlit[pos] = lit;
+                    a.tcid[pos] = cid;
+                }
+            });
+        __syncthreads();
+    }
+}
+
+// Pass 2: one block per bucket. Shared memory: 2^shift slot counters.
+__global__ void __launch_bounds__(OTB_LIST_THREADS) ot_bucket_lists_k(OtbArgs a) {
+    extern __shared__ u32 otb_cnt[];
+    __shared__ u32 warp_tot[OTB_LIST_THREADS / 32];
+    __shared__ u32 carry;
+    const u32 b = blockIdx.x;
+    const u32 l0 = b << a.shift;
+    const u32 D = a.c.D;
+    const u32 nl = D - l0 < (1u << a.shift) ? D - l0 : (1u << a.shift);
+    const u32 p0 = a.base[b], p1 = a.base[b + 1];
+    const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    for (u32 i = tid; i < nl; i += blockDim.x) otb_cnt[i] = 0;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (u32 k0 = p0; k0 < p1; k0 += blockDim.x) {
+        const u32 k = k0 + tid;
+        const bool valid = k < p1;
+        const u32 lit = valid ? __ldcs(&a.tlit[k]) : l0;
+        warp_smem_rank(otb_cnt, valid, lit - l0);
+    }
+    __syncthreads();
+    // block scan of the slot counts, blockDim.x slots per step: list sizes and starts
+    for (u32 i0 = 0; i0 < nl; i0 += blockDim.x) {
+        const u32 i = i0 + tid;
+        const u32 v = i < nl ? otb_cnt[i] : 0u;
+        u32 incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 t = __shfl_up_sync(OTB_FULL, incl, o);
+            if ((int)lane >= o) incl += t;
+        }
+        if (lane == 31) warp_tot[warp] = incl;
+        __syncthreads();
+        u32 before = carry;
+        for (u32 w = 0; w < warp; w++) before += warp_tot[w];
+        const u32 excl = before + incl - v;
+        if (i < nl) {
+            a.c.ot_size[l0 + i] = v;
+            a.c.ot_off[l0 + i] = p0 + excl;
+            otb_cnt[i] = excl;
+        }
+        __syncthreads();
+        if (tid == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+    for (u32 k0 = p0; k0 < p1; k0 += blockDim.x) {
+        const u32 k = k0 + tid;
+        const bool valid = k < p1;
+        const u32 lit = valid ? __ldcs(&a.tlit[k]) : l0;
+        const u32 cid = valid ? __ldcs(&a.tcid[k]) : 0u;
+        const u32 pos = warp_smem_rank(otb_cnt, valid, lit - l0);
+        if (valid) a.c.ot_refs[p0 + pos] = cid;
+    }
+}
+
+#endif  // SIGMA_CUDA
+
+}  // namespace sigma

@@ -11,7 +11,11 @@ namespace sigma {
 // extract() (src/cpu/simplify.cpp:95-113; GPU: transfer.cu:24-42 + prep_cnf_k,
 // kernels.cu:61-70): literals sorted ascending, signature over the clause,
 // status from the learnt flag. Rejects literals out of range and clauses that
-// repeat a variable.
+// repeat a variable. A one-literal clause is not a clause of the store: as the
+// reference's parser does (src/cpu/dimacs.cpp:153-159), its literal goes to the
+// trail (first claim of the variable wins; the opposite literal already there is
+// a contradiction) and the clause is kept as a deleted slot; the round then
+// propagates these units before its first phase.
 struct UploadArgs {
     Ctx c;
     const u64* off;      // num_clauses + 1
@@ -58,6 +62,13 @@ HD void k_upload_clause(const UploadArgs& a, u32 i) {
     h.size = n;
     h.sig = sig;
     h.flags = (a.learnt && a.learnt[i]) ? ST_LEARNT : ST_ORIGINAL;
+    if (n == 1) {
+        h.flags = ST_DELETED;
+        const u32 u = l[0];
+        const u32 old = atom_cas(&a.c.asg[ABS(u)], 0u, u);
+        if (old == 0) a.c.trail[atom_add(a.c.ntrail, 1u)] = u;
+        else if (old != u) set_unsat(a.c, ABS(u));
+    }
     a.c.hdr[i] = h;
 }
 

@@ -8,6 +8,7 @@
 #include "k_bce_ere.cuh"
 #include "k_bve.cuh"
 #include "k_lcve.cuh"
+#include "k_otb.cuh"
 #include "k_prop.cuh"
 #include "k_sortot.cuh"
 #include "k_store.cuh"
@@ -573,14 +574,72 @@ struct pf_sigma_ctx {
     }
 
     // ------------------------------------------------------------ stages
+#if SIGMA_CUDA
+    // Occurrence table by literal buckets (k_otb.cuh): buckets of 2^shift literal
+    // slots, at most OTB_MAX_BUCKETS of them (so up to 134M literal slots).
+    DBuf<u32> otb_count, otb_base, otb_cursor, otb_lit, otb_cid;
+    bool otb_plan(u32& shift, u32& nb) const {
+        u32 s = 8;
+        while (s < OTB_MAX_SHIFT && ((u64)D >> s) > 1024) s++;
+        shift = s;
+        nb = (u32)(((u64)D + (1ull << s) - 1) >> s);
+        return nb <= OTB_MAX_BUCKETS;
+    }
+    void create_ot_buckets(u32 shift, u32 nb) {
+        otb_count.reserve(rt, nb + 1);
+        otb_base.reserve(rt, nb + 1);
+        otb_cursor.reserve(rt, nb + 1);
+        otb_lit.reserve(rt, (size_t)nlits_used + 1);
+        otb_cid.reserve(rt, (size_t)nlits_used + 1);
+        rt.zero(otb_count.p, (size_t)nb * 4);
+        OtbArgs a{view(), shift, nb, otb_count.p, otb_cursor.p, otb_base.p, otb_lit.p, otb_cid.p};
+        static bool attr_set = false;
+        if (!attr_set) {
+            ck(cudaFuncSetAttribute(ot_bucket_lists_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)((1u << OTB_MAX_SHIFT) * 4)),
+               "smem attr");
+            attr_set = true;
+        }
+        const u32 grid = (u32)rt.sms * 8u;
+        if (ncls) {
+            rt.launches++;
+            ot_bucket_count_k<<<grid, 256, nb * 4, rt.stream>>>(a);
+            ck(cudaGetLastError(), "launch");
+        }
+        scan1_launch(otb_count.p, otb_base.p, nb, otb_base.p + nb);
+        rt.d2d(otb_cursor.p, otb_base.p, (size_t)nb * 4);
+        const u32 ntiles = (ncls + OTB_TILE - 1) / OTB_TILE;
+        if (ntiles) {
+            rt.launches++;
+            ot_bucket_fill_k<<<std::min(grid, ntiles), 256, 2 * nb * 4, rt.stream>>>(a);
+            ck(cudaGetLastError(), "launch");
+        }
+        rt.launches++;
+        ot_bucket_lists_k<<<nb, OTB_LIST_THREADS, (1u << shift) * 4, rt.stream>>>(a);
+        ck(cudaGetLastError(), "launch");
+        rt.d2d(ot_off.p + D, otb_base.p + nb, 4);
+    }
+#endif
+
     // createOT (simplify.cpp:35-56).
     void create_ot() {
-        Ctx c = view();
-        rt.zero(ot_size.p, (size_t)D * 4);
-        rt.each(FHist{c}, ncls);
         // the occurrences (live clauses' literals) never exceed the literal pool in
         // use, so the table is sized before its total is known
         if (nlits_used > ot_refs.n) ot_refs.reserve(rt, (size_t)nlits_used + nlits_used / 4 + 1024);
+#if SIGMA_CUDA
+        u32 shift = 0, nb = 0;
+        if (otb_plan(shift, nb)) {
+            create_ot_buckets(shift, nb);
+            word_to(ot_off.p + D, 0);
+            read_slots_checked();
+            ot_dirty = false;
+            alg_bytes += 2ull * (4ull * nlits_used + 8ull * ncls) + 8ull * D + 4ull * (u32)hr[0];
+            return;
+        }
+#endif
+        Ctx c = view();
+        rt.zero(ot_size.p, (size_t)D * 4);
+        rt.each(FHist{c}, ncls);
 #if SIGMA_CUDA
         scan1_launch(ot_size.p, ot_off.p, D, ot_off.p + D);
 #else
@@ -1240,10 +1299,25 @@ struct pf_sigma_ctx {
         return ms;
     }
 
+    // Units of the input (one-literal clauses) before the first phase: the
+    // reference's sigmifying() starts with rootify() + shrinkTop() (root-level
+    // propagation, then satisfied clauses dropped and false literals removed,
+    // src/cpu/simplify.cpp:163-164, shrink.cpp:152-216), so its first occurrence
+    // table holds only the clauses that survive them. Here: a table, the
+    // propagation, then a compaction of the store.
+    void root_units() {
+        if (prop_head >= ntrail) return;
+        timed(ST_OT, &pf_sigma_ctx::create_ot);
+        timed(ST_PROP, &pf_sigma_ctx::prop);
+        timed(ST_GC, &pf_sigma_ctx::gc);
+        compact = false;
+    }
+
     // sigmifying (simplify.cpp:182-209).
     void round() {
         phase = 0;
         mu_inc = 0;
+        root_units();
         count_all();
         i64 litsbefore = n_lits_after, diff = INT64_MAX;
         st.clauses_before = (u64)n_cls_after;
@@ -1493,6 +1567,7 @@ struct pf_sigma_ctx {
         std::fill(f_status.begin(), f_status.end(), (int)PF_OK);
         std::fill(f_phases.begin(), f_phases.end(), 0u);
         std::vector<uint8_t> done(nf, 0);
+        root_units();
         count_formulas();
         st.clauses_before = (u64)n_cls_after;
         st.literals_before = (u64)n_lits_after;
@@ -1838,6 +1913,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
             c.uploaded = false;
             return fail("invalid clause (empty, literal out of range or repeated variable)", PF_EINVAL);
         }
+        c.ntrail = c.read_u32(c.counters.p + 0);  // units of one-literal clauses
         c.uploaded = true;
         c.compact = false;
         return PF_OK;
@@ -2243,6 +2319,13 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
 #endif
     c.mis_big_a.free();
     c.mis_big_b.free();
+#if SIGMA_CUDA
+    c.otb_count.free();
+    c.otb_base.free();
+    c.otb_cursor.free();
+    c.otb_lit.free();
+    c.otb_cid.free();
+#endif
     c.pv_perm.free();
     c.pv_key.free();
     for (auto* b : b8) b->free();

@@ -51,6 +51,13 @@ CASES = [
      20_000),
     ("community_12k_s7_learnt", "community", dict(num_vars=4000, num_clauses=12000, communities=10, seed=7),
      dict(all=1, phases=3), 3_000),
+    # root-level units among the input clauses (propagated before the first phase)
+    ("aig_33k_s7_units", "with_units_of",
+     dict(gen="aig_tseitin", count=40, num_inputs=2000, num_and=30000, num_xor=3000, seed=7), dict(all=1)),
+    ("community_80k_s8_units", "with_units_of",
+     dict(gen="community", count=100, num_vars=20000, num_clauses=80000, communities=20, seed=8), dict(all=1)),
+    ("ksat3_2k_s9_units", "with_units_of", dict(gen="random_ksat", count=120, unit_seed=6, num_vars=2000,
+                                                num_clauses=7000, k=3, seed=9), dict(all=1)),
 ]
 
 SMALL = 20_000  # keep full clause lists below this many output clauses

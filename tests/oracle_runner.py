@@ -20,6 +20,7 @@ from parafrost_gb300.options import Options
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "libsigma_oracle.so")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "sigma_ref")
+REF_SOLVER = os.path.join(ROOT, "oracle", "_ref", "parafrost")
 
 _lib = None
 
@@ -109,3 +110,38 @@ def run_reference(num_vars, lits, offsets, opts: Options | None = None, level: i
         args += opts.reference_flags()
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
         return rounddump.read(dump)
+
+
+def solver_available() -> bool:
+    return os.path.exists(REF_SOLVER)
+
+
+def reference_solve(num_vars, lits, offsets, units=(), timeout: float = 600.0):
+    """Solve a formula (plus unit clauses) with the compiled reference CDCL solver,
+    its own simplifier off (-no-sigma -no-sigmalive). Returns ("SAT", model) with
+    model a uint8 array over variables 0..num_vars (1 = true), or ("UNSAT", None)."""
+    lits = np.ascontiguousarray(lits, dtype=np.uint32)
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+    units = np.asarray(units, dtype=np.uint32)
+    if units.size:
+        lits = np.concatenate([lits[int(offsets[0]):int(offsets[-1])], units])
+        offsets = np.concatenate([offsets - offsets[0], offsets[-1] - offsets[0] + 1 + np.arange(units.size, dtype=np.uint64)])
+    with tempfile.TemporaryDirectory() as td:
+        cnf = os.path.join(td, "f.cnf")
+        cnfgen.to_dimacs(cnf, num_vars, lits, offsets)
+        out = subprocess.run([REF_SOLVER, cnf, "-quiet", "-no-sigma", "-no-sigmalive", "-model", "-modelprint"],
+                             check=True, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                             timeout=timeout).stdout
+    status = [l.split()[1] for l in out.splitlines() if l.startswith("s ")]
+    if status == ["UNSATISFIABLE"]:
+        return "UNSAT", None
+    if status != ["SATISFIABLE"]:
+        raise RuntimeError(f"reference solver answered {status}")
+    model = np.zeros(num_vars + 1, dtype=np.uint8)
+    for line in out.splitlines():
+        if line.startswith("v "):
+            for tok in line.split()[1:]:
+                x = int(tok)
+                if x > 0:
+                    model[x] = 1
+    return "SAT", model

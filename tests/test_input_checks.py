@@ -94,3 +94,24 @@ def test_create_ot_rejects_bad_offsets_gpu(cuda_lib):
 @pytest.mark.gpu
 def test_loop_limit_times_out_gpu(cuda_lib):
     _check_loop_limit(cuda_lib)
+
+
+def _check_conflicting_units(lib):
+    """(x) and (-x) among the input clauses: the round proves UNSAT. (The reference's
+    parser drops a clause that earlier units falsify, src/cpu/dimacs.cpp:153-176, and
+    goes on as if it were absent; a round here never drops a clause.)"""
+    nv, lits, off = cnfgen.random_ksat(200, 600, 3, seed=2)
+    lits = np.concatenate([lits, np.array([2 * 17, 2 * 17 + 1], dtype=np.uint32)])
+    off = np.concatenate([off, off[-1] + np.array([1, 2], dtype=np.uint64)])
+    with Simplifier(Options(all=1), library=lib) as s:
+        s.awaken(nv, lits, off)
+        assert s.sigmify().status == 1
+
+
+def test_conflicting_input_units_emu(built):
+    _check_conflicting_units(built["emu"])
+
+
+@pytest.mark.gpu
+def test_conflicting_input_units_gpu(cuda_lib):
+    _check_conflicting_units(cuda_lib)
