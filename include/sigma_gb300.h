@@ -139,6 +139,19 @@ pf_status pf_sigma_result_sizes(pf_sigma_ctx* ctx, uint64_t* num_clauses, uint64
 pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets, uint8_t* learnt,
                             uint32_t* units, uint32_t* resolved, uint8_t* eliminated);
 
+/* Model extension on the device (MODEL::extend, src/cpu/model.cpp:104-138) after a
+ * round that ended PF_OK: values holds, per variable, the caller's model of the
+ * simplified formula (1 true, 0 false) and receives a model of the original formula.
+ * The round's units are set and eliminated variables start false (as the reference,
+ * whose solver never assigns them), then the witness stack is walked from its end:
+ * a record whose other literals are all false sets its witness true. Single formula:
+ * values[0 .. num_vars] (index 0 unused); its records form one dependent chain,
+ * walked by one device thread. Formula batch: formula after formula, num_vars[f] + 1
+ * entries each (the first unused; the layout of pf_sigma_batch_download's eliminated
+ * flags), every formula walked by its own thread, side by side. For the batched
+ * SAT answers of many formulas; one large formula is faster on a host core. */
+pf_status pf_sigma_extend(pf_sigma_ctx* ctx, uint8_t* values);
+
 /* Writes the per-stage round dump of the last round to path (dump_level > 0). */
 pf_status pf_sigma_write_dump(pf_sigma_ctx* ctx, const char* path);
 

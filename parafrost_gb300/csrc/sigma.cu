@@ -8,6 +8,7 @@
 #include "k_bce_ere.cuh"
 #include "k_bve.cuh"
 #include "k_lcve.cuh"
+#include "k_model.cuh"
 #include "k_otb.cuh"
 #include "k_prop.cuh"
 #include "k_sortot.cuh"
@@ -175,6 +176,24 @@ struct FRecGather {
         o[n - 1] = c.resolved[st + n - 1];
     }
 };
+// Model extension: records per formula, and the walks.
+struct FRecCount {
+    Ctx c; const u32* rstart; u32* f_recs;
+    HD void operator()(u32 r) const { atom_add(&f_recs[c.var_fid[ABS(c.resolved[rstart[r]])]], 1u); }
+};
+struct FExtendFormula { ExtendArgs a; HD void operator()(u32 f) const { k_extend_formula(a, f); } };
+struct FExtendSingle { ExtendArgs a; HD void operator()() const { k_extend_single(a); } };
+struct FExtendClear { Ctx c; uint8_t* value; HD void operator()(u32 v) const { k_extend_clear(c, value, v); } };
+struct FExtendUnit { Ctx c; uint8_t* value; HD void operator()(u32 i) const { k_extend_unit(c, value, i); } };
+struct FExtendIn {
+    ExtendMap m; const uint8_t* packed; uint8_t* value;
+    HD void operator()(u32 p) const { k_extend_in(m, packed, value, p); }
+};
+struct FExtendOut {
+    ExtendMap m; const uint8_t* value; uint8_t* packed;
+    HD void operator()(u32 p) const { k_extend_out(m, value, packed, p); }
+};
+
 // Trail split: formula and index of every unit; units per formula.
 struct FUnitFid {
     Ctx c; u32* key; u32* val; u64* f_units;
@@ -238,6 +257,7 @@ struct pf_sigma_ctx {
     Runtime rt;
     StageTimer tm;
     bool uploaded = false, has_learnt = false;
+    u32 rounds_run = 0;  // rounds since the last upload
     u32 nvars = 0, D = 0;
     u32 ncls = 0;
     u64 nlits_used = 0;
@@ -1459,6 +1479,86 @@ struct pf_sigma_ctx {
         rt.d2h(h_out, out.p, (size_t)w * 4);
     }
 
+    // MODEL::extend (src/cpu/model.cpp:104-138) on the device for the last round's
+    // result: h_values holds the caller's model of the simplified formula(s) and
+    // receives the model of the original one(s). A batch's formulas are walked side
+    // by side, one thread each.
+    void extend(uint8_t* h_values) {
+        DBuf<uint8_t> val, packed;
+        DBuf<u64> pfirst;
+        val.reserve(rt, (size_t)nvars + 1);
+        ExtendMap m{nullptr, nf ? f_var.p : nullptr, nf};
+        u64 npacked = 0;
+        if (!nf) {
+            rt.h2d(val.p, h_values, (size_t)nvars + 1);
+        } else {
+            std::vector<u64> first(nf + 1, 0);
+            for (u32 f = 0; f < nf; f++) first[f + 1] = first[f] + h_f_nv[f] + 1;
+            npacked = first[nf];
+            if (npacked >= 0xFFFFFFF0ull) throw std::runtime_error("batch values exceed 32-bit positions");
+            pfirst.reserve(rt, nf + 1);
+            rt.h2d(pfirst.p, first.data(), (size_t)(nf + 1) * 8);
+            packed.reserve(rt, npacked);
+            rt.h2d(packed.p, h_values, npacked);
+            rt.zero(val.p, (size_t)nvars + 1);
+            m.p_first = pfirst.p;
+            rt.each(FExtendIn{m, packed.p, val.p}, (u32)npacked);
+        }
+        const Ctx c = view();
+        rt.each(FExtendClear{c, val.p}, nvars + 1);
+        if (ntrail) rt.each(FExtendUnit{c, val.p}, ntrail);
+        ExtendArgs a{};
+        a.resolved = resolved.p;
+        a.value = val.p;
+        a.nres = nresolved;
+        a.err = counters.p + 1;
+        DBuf<u32> flag, scan, rstart, key, ord, k2, v2, frec, ffirst;
+        DBuf<u64> words, fw;
+        if (!nf) {
+            if (nresolved) rt.one(FExtendSingle{a});
+        } else if (nresolved) {
+            if (nresolved >= 0xFFFFFFF0ull) throw std::runtime_error("witness stack too large for 32-bit positions");
+            const u32 w = (u32)nresolved;
+            flag.reserve(rt, w);
+            scan.reserve(rt, w);
+            rt.each(FRecStart{res_mark.p, flag.p}, w);
+            const u32 R = scan32(flag.p, scan.p, w);
+            rstart.reserve(rt, R + 1);
+            rt.each(FRecScatter{flag.p, scan.p, rstart.p}, w);
+            key.reserve(rt, R + 1);
+            ord.reserve(rt, R + 1);
+            words.reserve(rt, R + 1);
+            fw.reserve(rt, nf);
+            rt.zero(fw.p, (size_t)nf * 8);
+            rt.each(FRecFid{c, rstart.p, R, w, key.p, ord.p, words.p, fw.p}, R);
+            k2.reserve(rt, R + 1);
+            v2.reserve(rt, R + 1);
+            radix_hist.reserve(rt, radix_hist_elems(R));
+            radix_hscan.reserve(rt, radix_hist_elems(R));
+            scan_tmp32.reserve(rt, scan_tmp_elems(radix_hist_elems(R)) + 4);
+            const int bits = fid_bits();
+            radix_sort_pairs(key.p, ord.p, k2.p, v2.p, R, bits, radix_hist.p, radix_hscan.p, scan_tmp32.p, rt.stream);
+            rt.launches += 5 * (bits / 8);
+            frec.reserve(rt, nf + 1);
+            ffirst.reserve(rt, nf + 1);
+            rt.zero(frec.p, (size_t)(nf + 1) * 4);
+            rt.each(FRecCount{c, rstart.p, frec.p}, R);
+            write_u32(ffirst.p + nf, scan32(frec.p, ffirst.p, nf));
+            a.rec_start = rstart.p;
+            a.rec_words = words.p;
+            a.order = ord.p;
+            a.f_first = ffirst.p;
+            rt.each(FExtendFormula{a}, nf);
+        }
+        check();
+        if (!nf) {
+            rt.d2h(h_values, val.p, (size_t)nvars + 1);
+        } else {
+            rt.each(FExtendOut{m, val.p, packed.p}, (u32)npacked);
+            rt.d2h(h_values, packed.p, npacked);
+        }
+    }
+
     // Trail units grouped per formula, in the formula's numbering.
     void batch_units(std::vector<u64>& f_units_out, u32* h_out) {
         f_units_out.assign(nf, 0);
@@ -1915,6 +2015,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         }
         c.ntrail = c.read_u32(c.counters.p + 0);  // units of one-literal clauses
         c.uploaded = true;
+        c.rounds_run = 0;
         c.compact = false;
         return PF_OK;
     });
@@ -2032,6 +2133,7 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     }
     if (c.opt.dump_level > 0) c.rec(11, 0, 8, {status == PF_OK ? 0u : (status == PF_UNSAT ? 1u : 3u)});
     c.st.status = status;
+    c.rounds_run++;
     c.st.clauses_after = (u64)c.n_cls_after;
     c.st.literals_after = (u64)c.n_lits_after;
     c.st.units = c.ntrail;
@@ -2149,6 +2251,16 @@ pf_status pf_sigma_batch_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* o
                 w += c.h_f_nv[f];
             }
         }
+        return PF_OK;
+    });
+}
+
+pf_status pf_sigma_extend(pf_sigma_ctx* ctx, uint8_t* values) {
+    if (!ctx || !values) return fail("null argument", PF_EINVAL);
+    if (!ctx->uploaded || ctx->st.status != PF_OK || !ctx->rounds_run)
+        return fail("model extension needs a finished round without contradiction", PF_ESTATE);
+    return guarded([&]() -> pf_status {
+        ctx->extend(values);
         return PF_OK;
     });
 }

@@ -86,6 +86,8 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     lib.pf_sigma_result_sizes.restype = ctypes.c_int
     lib.pf_sigma_download.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
     lib.pf_sigma_download.restype = ctypes.c_int
+    lib.pf_sigma_extend.argtypes = [_VP, _VP]
+    lib.pf_sigma_extend.restype = ctypes.c_int
     lib.pf_sigma_write_dump.argtypes = [_VP, ctypes.c_char_p]
     lib.pf_sigma_write_dump.restype = ctypes.c_int
     lib.pf_sigma_upload_batch.argtypes = [_VP, _U32, _VP, _VP, _VP, _VP]
@@ -321,6 +323,31 @@ class Simplifier:
                          learnt[c0:c1], units[u0:u1], resolved[r0:r1], elim[e0:e1])
             out.append((int(st[f]), int(ph[f]), res))
             c0, u0, r0, e0 = c1, u1, r1, e1
+        return out
+
+    def extend(self, values: np.ndarray) -> np.ndarray:
+        """MODEL::extend on the device for the single formula of the last round:
+        values (uint8 per variable 0..num_vars, 1 = true) is a model of the simplified
+        formula; returns a model of the original formula."""
+        v = np.array(values, dtype=np.uint8, copy=True)
+        assert v.size == self.num_vars + 1
+        self._check(self.lib.pf_sigma_extend(self.h, _ptr(v)))
+        return v
+
+    def batch_extend(self, models: list) -> list:
+        """MODEL::extend on the device for every formula of the last batched round:
+        models[f] (uint8 per variable 0..num_vars[f]) is a model of formula f's
+        simplified result; returns the extended models, formulas walked side by side."""
+        nf = self.batch_vars.size
+        assert len(models) == nf
+        packed = np.concatenate([np.asarray(m, dtype=np.uint8) for m in models]) if nf else np.zeros(0, np.uint8)
+        assert packed.size == int(self.batch_vars.astype(np.uint64).sum()) + nf
+        self._check(self.lib.pf_sigma_extend(self.h, _ptr(packed)))
+        out, e0 = [], 0
+        for f in range(nf):
+            e1 = e0 + int(self.batch_vars[f]) + 1
+            out.append(packed[e0:e1])
+            e0 = e1
         return out
 
     def write_dump(self, path: str) -> None:
