@@ -31,4 +31,11 @@ $(OUT)/sigma_ref: oracle/ref_harness.cpp $(OUT)/libpfref.a
 $(OUT)/parafrost: $(SRCDIR)/main.cpp $(OUT)/libpfref.a
 	$(CXX) $(CXXFLAGS) -I$(SRCDIR) $< -o $@ $(OUT)/libpfref.a
 
-.PHONY: all
+# the reference solver with its preprocessing round handed to this repository's C ABI
+# (oracle/dropin_harness.cpp), linked to the kernel-logic emulation build
+EMU := parafrost_gb300/_lib/libsigma_emu.so
+dropin: $(OUT)/sigma_dropin
+$(OUT)/sigma_dropin: oracle/dropin_harness.cpp include/sigma_gb300.hpp include/sigma_gb300.h $(OUT)/libpfref.a $(EMU)
+	$(CXX) $(CXXFLAGS) -I$(SRCDIR) -Iinclude $< -o $@ $(OUT)/libpfref.a $(abspath $(EMU)) -Wl,-rpath,$(abspath $(dir $(EMU)))
+
+.PHONY: all dropin

@@ -90,6 +90,17 @@ def build_reference(refdir: str | None = None) -> str | None:
     return os.path.join(ROOT, "oracle", "_ref", "sigma_ref")
 
 
+def build_dropin(refdir: str | None = None) -> str | None:
+    """Compile the drop-in harness (the reference solver calling this repository's C
+    ABI through include/sigma_gb300.hpp, linked to the emulation build) when the
+    reference sources exist."""
+    refdir = refdir or os.environ.get("PARAFROST_REF")
+    if not refdir or not os.path.isdir(os.path.join(refdir, "src", "cpu")):
+        return None
+    _run(["make", "-s", "-f", os.path.join("oracle", "ref.mk"), f"REFDIR={refdir}", "dropin"])
+    return os.path.join(ROOT, "oracle", "_ref", "sigma_dropin")
+
+
 def build_all(with_cuda: bool = True, refdir: str | None = None) -> dict:
     out = {}
     jobs = {"oracle": build_oracle, "emu": build_emu}
@@ -101,4 +112,5 @@ def build_all(with_cuda: bool = True, refdir: str | None = None) -> dict:
         for k, f in futs.items():
             out[k] = f.result()
         out["reference"] = ref.result()
+    out["dropin"] = build_dropin(refdir) if out["reference"] else None
     return out
