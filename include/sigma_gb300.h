@@ -63,7 +63,9 @@ typedef struct {
                               * waves) before the round gives up with PF_ETIMEOUT; 0: the
                               * default bound, variables + 2, which a correct round never reaches.
                               * A small value exercises the give-up path without any wait. */
-    int32_t reserved[6];
+    int32_t proof;           /* "proof" = 0: 1 records the round's DRAT proof (pf_sigma_proof);
+                              * single formulas only */
+    int32_t reserved[5];
 } pf_options;
 
 /* Per-round statistics (the reference's stage report, src/cpu/statistics.cpp:28-41,
@@ -151,6 +153,19 @@ pf_status pf_sigma_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets
  * flags), every formula walked by its own thread, side by side. For the batched
  * SAT answers of many formulas; one large formula is faster on a host core. */
 pf_status pf_sigma_extend(pf_sigma_ctx* ctx, uint8_t* values);
+
+/* The last round's DRAT proof in the reference's binary format (src/cpu/proof.cpp:
+ * 95-135, the file ParaFROST writes with -proof): one addition line per clause the
+ * round derived (strengthened by SUB, substituted by an equivalence, resolvents of
+ * VE) and per unit it assigned, and one deletion line per clause that SUB found
+ * subsumed or ERE redundant, as they happen, then the empty clause when the round
+ * proved UNSAT. Literals are in the caller's numbering. The reference leaves out an
+ * added clause that a unit assigned before it satisfies; this one keeps it. Lines of one stage come in any order (the stage's
+ * variables are independent); every line is implied by unit propagation over the
+ * input and the lines before it. Needs the option proof = 1. out may be NULL: *bytes
+ * receives the size; otherwise *bytes is out's capacity on entry and the size on
+ * return. */
+pf_status pf_sigma_proof(pf_sigma_ctx* ctx, uint8_t* out, uint64_t* bytes);
 
 /* Writes the per-stage round dump of the last round to path (dump_level > 0). */
 pf_status pf_sigma_write_dump(pf_sigma_ctx* ctx, const char* path);

@@ -29,6 +29,7 @@ enum Kind : uint32_t {
     K_COUNTS = 10,  // n_cls_after, n_lits_after
     K_STATUS = 11,  // 0 = round finished, 1 = UNSAT proved inside the round
     K_TIMING = 12,  // microseconds (not compared)
+    K_PROOFMARK = 13,  // proof lines written before the round (reference harness with -proof)
 };
 
 enum Stage : uint32_t {

@@ -9,6 +9,8 @@
  * wall-clock timer around the phase loop (src/cpu/simplify.cpp:182-209).
  *
  * usage: sigma_ref <cnf.dimacs> <dump.bin> <level> [--learnt-tail=N] [reference options...]
+ *   with the reference options -proof --proofout=<file>, the reference writes its
+ *   binary DRAT proof; the dump then records how many lines precede the round.
  *   level 0: input + final state + timing; 1: + per-phase summaries; 2: + every stage.
  *   --learnt-tail=N: the last N parsed clauses become learnt clauses before the
  *   round (an inprocessing call's input: awaken() extracts the original clauses,
@@ -118,6 +120,8 @@ struct Harness : public ParaFROST {
 
     // ParaFROST::sigmifying() (src/cpu/simplify.cpp:157-232) up to the write-back.
     void round() {
+        // with -proof, the lines written so far (the parser's) are not the round's
+        if (opts.proof_en) g_dump.rec(sigdump::K_PROOFMARK, 0, sigdump::S_INPUT, {(uint32_t)proof.numClauses()});
         rootify();
         shrinkTop(false);
         if (orgs.empty()) {

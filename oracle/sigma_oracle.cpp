@@ -1265,3 +1265,139 @@ extern "C" long oracle_extend_and_check(uint32_t num_vars, uint8_t* value, const
     }
     return bad;
 }
+
+// ---------------------------------------------------------------- DRAT check
+// A forward checker for the addition lines of a binary DRAT proof (the format of
+// src/cpu/proof.cpp:95-135): every added clause must follow by unit propagation
+// (RUP) from the input clauses and the clauses added before it. Deletion lines are
+// skipped (a round adds none). Watched-literal propagation, root assignments kept.
+namespace {
+struct RupChecker {
+    std::vector<std::vector<u32>> cls;
+    std::vector<std::vector<u32>> watch;  // per literal: clause indices watching it
+    std::vector<int8_t> val;              // per literal: 1 true, 0 false, -1 unassigned
+    std::vector<u32> trail;
+    size_t head = 0;
+    bool root_conflict = false;
+
+    explicit RupChecker(uint32_t nv) : watch(2 * (size_t)nv + 2), val(2 * (size_t)nv + 2, -1) {}
+    bool assign(u32 lit) {
+        if (val[lit] == 1) return true;
+        if (val[lit] == 0) return false;
+        val[lit] = 1;
+        val[lit ^ 1u] = 0;
+        trail.push_back(lit);
+        return true;
+    }
+    // unit propagation from trail[head]; false on a conflict
+    bool propagate() {
+        while (head < trail.size()) {
+            const u32 f = trail[head++] ^ 1u;  // the literal that became false
+            std::vector<u32>& ws = watch[f];
+            size_t j = 0;
+            bool conflict = false;
+            for (size_t i = 0; i < ws.size(); i++) {
+                const u32 ci = ws[i];
+                if (conflict) { ws[j++] = ci; continue; }
+                std::vector<u32>& c = cls[ci];
+                if (c[0] == f) std::swap(c[0], c[1]);
+                if (val[c[0]] == 1) { ws[j++] = ci; continue; }
+                bool moved = false;
+                for (size_t k = 2; k < c.size(); k++) {
+                    if (val[c[k]] != 0) {
+                        std::swap(c[1], c[k]);
+                        watch[c[1]].push_back(ci);
+                        moved = true;
+                        break;
+                    }
+                }
+                if (moved) continue;
+                ws[j++] = ci;
+                if (val[c[0]] == 0) conflict = true;
+                else assign(c[0]);
+            }
+            ws.resize(j);
+            if (conflict) return false;
+        }
+        return true;
+    }
+    void add(const std::vector<u32>& lits) {
+        if (root_conflict) return;
+        if (lits.empty()) { root_conflict = true; return; }
+        if (lits.size() == 1) {
+            if (!assign(lits[0]) || !propagate()) root_conflict = true;
+            return;
+        }
+        std::vector<u32> c(lits);
+        // watch two literals that are not false where possible
+        for (size_t k = 0; k < 2; k++)
+            for (size_t m = k; m < c.size(); m++)
+                if (val[c[m]] != 0) { std::swap(c[k], c[m]); break; }
+        const u32 ci = (u32)cls.size();
+        cls.push_back(c);
+        watch[c[0]].push_back(ci);
+        watch[c[1]].push_back(ci);
+        if (val[c[0]] == 0) root_conflict = true;  // every literal false at the root
+        else if (val[c[1]] == 0 && val[c[0]] != 1) {
+            if (!assign(c[0]) || !propagate()) root_conflict = true;
+        }
+    }
+    bool rup(const std::vector<u32>& lits) {
+        if (root_conflict) return true;
+        const size_t mark = trail.size(), mhead = head;
+        bool ok = false;
+        for (u32 l : lits) {
+            if (val[l] == 1) { ok = true; break; }
+            if (val[l] == -1) assign(l ^ 1u);
+        }
+        if (!ok) ok = !propagate();
+        for (size_t i = trail.size(); i-- > mark;) { val[trail[i]] = -1; val[trail[i] ^ 1u] = -1; }
+        trail.resize(mark);
+        head = mhead;
+        return ok;
+    }
+};
+}  // namespace
+
+/* Checks every addition line of a binary DRAT proof by RUP against the formula and
+ * the earlier lines. Returns -1 when all hold (sets *empty to 1 when an empty clause
+ * is added, i.e. the proof refutes the formula), else the index of the first line
+ * that fails; -2 for a malformed proof. */
+extern "C" long oracle_check_drat(uint32_t num_vars, const uint32_t* lits, const uint64_t* offsets,
+                                  uint64_t num_clauses, const uint8_t* proof, uint64_t nbytes, int* empty) {
+    RupChecker ck(num_vars);
+    std::vector<u32> c;
+    for (uint64_t i = 0; i < num_clauses; i++) {
+        c.assign(lits + offsets[i], lits + offsets[i + 1]);
+        ck.add(c);
+    }
+    if (empty) *empty = 0;
+    uint64_t p = 0;
+    long line = 0;
+    while (p < nbytes) {
+        const uint8_t tag = proof[p++];
+        if (tag != 'a' && tag != 'd') return -2;
+        c.clear();
+        while (true) {
+            if (p >= nbytes) return -2;
+            u32 r = 0, shift = 0;
+            uint8_t b;
+            do {
+                if (p >= nbytes || shift > 28) return -2;
+                b = proof[p++];
+                r |= (u32)(b & 127u) << shift;
+                shift += 7;
+            } while (b & 128u);
+            if (r == 0) break;
+            if ((r >> 1) > num_vars || r < 2) return -2;
+            c.push_back(r);
+        }
+        if (tag == 'a') {
+            if (!ck.rup(c)) return line;
+            if (c.empty() && empty) *empty = 1;
+            ck.add(c);
+        }
+        line++;
+    }
+    return -1;
+}

@@ -81,11 +81,39 @@ struct Ctx {
     // (deletion and creation included), and this phase's stamp
     u32* cstamp;
     u32 stamp;
+    // DRAT proof lines of the round (null when no proof is recorded): words
+    // [n, lit_0 .. lit_{n-1}] per added clause, appended at a device counter
+    u32* proof;
+    u64* nproof;
+    u64 cap_proof;
 };
 
 constexpr u32 NONE = 0xFFFFFFFFu;
 
 // Clause r's literals or status changed in this phase.
+// One line of the proof: an added clause (the reference's proof.addResolvent /
+// addUnit, src/cpu/proof.cpp:181-228, for a strengthened, substituted or resolved
+// clause or a unit) or, with del, a deleted one (proof.deleteClause, proof.cpp:
+// 193, through removeClause, src/cpu/sclause.cpp:67-84). Header word: the size,
+// with bit 31 set for a deletion.
+constexpr u32 PROOF_DELETE = 0x80000000u;
+HD void proof_line(const Ctx& c, const u32* lits, u32 n, bool del = false) {
+    if (!c.proof) return;
+    const u64 pos = atom_add64(c.nproof, (u64)n + 1);
+    if (pos + n + 1 > c.cap_proof) {
+        atom_or(c.err, ERR_CAP_SCRATCH);  // the proof buffer was sized too small
+        return;
+    }
+    c.proof[pos] = n | (del ? PROOF_DELETE : 0u);
+    for (u32 i = 0; i < n; i++) c.proof[pos + 1 + i] = lits[i];
+}
+// removeClause's proof line for live clause r (subsumed, or made redundant by ERE).
+HD void proof_delete(const Ctx& c, u32 r) {
+    if (!c.proof) return;
+    const Hdr h = c.hdr[r];
+    proof_line(c, c.lits + h.start, h.size, true);
+}
+
 HD void touch(const Ctx& c, u32 r) {
     if (c.cstamp) c.cstamp[r] = c.stamp;
 }

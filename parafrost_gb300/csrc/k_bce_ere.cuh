@@ -258,8 +258,10 @@ HD void k_ere_pair(const EreArgs& a, const u32* perm, const u64* off, u32 npos, 
 // are collected for the ordered fix-up.
 HD void k_ere_resolve(const EreArgs& a, u32 q) {
     const u32 t = a.rec_target[q];
-    if (a.claim[t] == a.rec_key[q]) mark_deleted(a.c, t);
-    else {
+    if (a.claim[t] == a.rec_key[q]) {
+        proof_delete(a.c, t);
+        mark_deleted(a.c, t);
+    } else {
         const u32 pos = atom_add(a.nlosers, 1u);
         a.losers[pos] = q;
     }
@@ -278,7 +280,10 @@ HD void ere_fixup(const EreArgs& a, const u64* keys, u32 nkeys) {
         if (c.ot_size[dx] > c.ot_size[fx]) swap_t(dx, fx);
         const ListRef me = list_of(c, dx), other = list_of(c, fx);
         const u32 t = ere_find(c, v, c.hdr[me.ids[i]], c.hdr[other.ids[j]], a.ere_clause_max);
-        if (t != NONE) mark_deleted(c, t);
+        if (t != NONE) {
+            proof_delete(c, t);
+            mark_deleted(c, t);
+        }
     }
 }
 
@@ -297,7 +302,10 @@ HD void ere_sequential(const EreArgs& a) {
             for (u32 j = 0; j < other.n; j++) {
                 if (h_deleted(c.hdr[other.ids[j]].flags)) continue;
                 const u32 t = ere_find(c, v, c.hdr[me.ids[i]], c.hdr[other.ids[j]], a.ere_clause_max);
-                if (t != NONE) mark_deleted(c, t);
+                if (t != NONE) {
+                    proof_delete(c, t);
+                    mark_deleted(c, t);
+                }
             }
         }
     }

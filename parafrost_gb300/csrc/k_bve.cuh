@@ -209,6 +209,7 @@ HD void enqueue_unit(const Ctx& c, u32 u) {
     if (old == 0) {
         const u32 pos = atom_add(c.ntrail, 1u);
         c.trail[pos] = u;
+        proof_line(c, &u, 1);  // learnUnit's proof.addUnit (src/cpu/solve.h:475-479)
     } else if (old != u) {
         set_unsat(c, ABS(u));
     }
@@ -250,6 +251,7 @@ HD u32 substitute_clause(const Ctx& c, u32 r, u32 dx, u32 def) {
     h.sig = calc_sig(l, n);
     c.hdr[r].size = h.size;
     c.hdr[r].sig = h.sig;
+    proof_line(c, l, n);
     return 0;
 }
 

@@ -151,6 +151,7 @@ HD void prop_clause(const PropArgs& a, u32 k) {
         if (old == 0) {
             const u32 pos = atom_add(c.ntrail, 1u);
             c.trail[pos] = u;
+            proof_line(c, &u, 1);  // learnUnit's proof.addUnit (src/cpu/solve.h:475-479)
         } else if (old != u) {
             set_unsat(c, ABS(u));
         }

@@ -126,6 +126,7 @@ HD void sub_strengthen(const SubArgs& a, u32 k, u32 p, u32 r, u32 me, SubLocal& 
     c.hdr[r].sig = h.sig;
     c.hdr[r].size = h.size;
     touch(c, r);
+    if (n > 1) proof_line(c, l, n);
     if (n == 1) {
         const u32 unit = l[0];
         int val = lit_value(c, unit);
@@ -160,6 +161,7 @@ HD bool sub_subsume(const Ctx& c, const u32* list, u32 end, u32 cr) {
                 c.hdr[sr].flags = (s.flags & ~3u) | ST_ORIGINAL;
                 touch(c, sr);
             }
+            proof_delete(c, cr);
             mark_deleted(c, cr);
             return true;
         }

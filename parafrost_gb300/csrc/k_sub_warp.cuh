@@ -59,6 +59,7 @@ HD void sub_warp_side(const SubArgs& a, u32 k, u32 p, u32 lx, u32 lo, SubLocal& 
                     c.hdr[sr].flags = (s.flags & ~3u) | ST_ORIGINAL;
                     touch(c, sr);
                 }
+                proof_delete(c, r);
                 mark_deleted(c, r);
             });
         }

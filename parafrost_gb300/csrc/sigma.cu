@@ -60,6 +60,14 @@ struct FMisBound { LcveArgs a; HD void operator()(u32 i) const { k_mis_bound(a, 
 struct FElectFlag { LcveArgs a; u32* flags; HD void operator()(u32 i) const { k_elect_flag(a, flags, i); } };
 struct FElectWrite { LcveArgs a; const u32* flags; const u32* scan; HD void operator()(u32 i) const { k_elect_write(a, flags, scan, i); } };
 struct FFill32 { u32* p; u32 v; HD void operator()(u32 i) const { p[i] = v; } };
+// Proof line of clause from + i (a resolvent just written).
+struct FProofClause {
+    Ctx c; u32 from;
+    HD void operator()(u32 i) const {
+        const Hdr h = c.hdr[from + i];
+        if (!h_deleted(h.flags) && h.size > 1) proof_line(c, c.lits + h.start, h.size);
+    }
+};
 struct FSortList { SortArgs a; HD void operator()(u32 i) const { k_sort_list(a, i); } };
 struct FSubPossible { SubArgs a; u32* flag; HD void operator()(u32 i) const { k_sub_unit_possible(a, flag, i); } };
 struct FSubPv { SubArgs a; HD void operator()(u32 i) const { k_sub_pv(a, i); } };
@@ -256,6 +264,11 @@ struct pf_sigma_ctx {
     pf_options opt;
     Runtime rt;
     StageTimer tm;
+    // DRAT proof of the round (opt.proof): lines [n, lits...] written by the kernels
+    // into `proof` at the device counter counters64[4] (units as they are assigned);
+    // proof_bound bounds the words reserved so far
+    DBuf<u32> proof;
+    u64 proof_bound = 0;
     bool uploaded = false, has_learnt = false;
     u32 rounds_run = 0;  // rounds since the last upload
     u32 nvars = 0, D = 0;
@@ -364,6 +377,9 @@ struct pf_sigma_ctx {
         c.res_mark = nf ? res_mark.p : nullptr;
         c.cstamp = cstamp.p;
         c.stamp = (u32)phase + 1u;
+        c.proof = opt.proof ? proof.p : nullptr;
+        c.nproof = opt.proof ? counters64.p + 4 : nullptr;
+        c.cap_proof = proof.n;
         return c;
     }
 
@@ -568,6 +584,19 @@ struct pf_sigma_ctx {
         if (e & ERR_ITER) throw int(PF_ETIMEOUT);
         if (e & ERR_INPUT) throw int(PF_EINVAL);
         if (e & ERR_INTERNAL) throw std::runtime_error("internal invariant violated");
+    }
+
+    // ------------------------------------------------------------ proof
+    // Room for `words` more proof words (the buffer keeps what is written).
+    void proof_reserve(u64 words) {
+        if (!opt.proof) return;
+        proof_bound += words;
+        if (proof_bound > proof.n) proof.grow(rt, (size_t)(proof_bound + proof_bound / 2 + 4096), proof.n);
+    }
+    // Resolvents written in [from, ncls): each a proof line, in store order.
+    void proof_clauses(u32 from) {
+        if (!opt.proof || from >= ncls) return;
+        rt.each(FProofClause{view(), from}, ncls - from);
     }
 
     // ------------------------------------------------------------ capacity
@@ -892,6 +921,7 @@ struct pf_sigma_ctx {
     // SUB (elimination.cpp:110-129).
     void sub() {
         if (!(opt.sub || opt.ve_plus) || !npvs) return;
+        proof_reserve(phase_ws / 2 + 16);  // at most two lines per clause of the elected lists
         SubArgs a;
         a.c = view();
         a.pvs = pvs.p;
@@ -1110,6 +1140,8 @@ struct pf_sigma_ctx {
         ensure_clauses((u64)ncls + add_cls);
         ensure_lits(nlits_used + add_lits);
         ensure_resolved(nresolved + add_wit);
+        // substituted clauses (one line each) and the resolvents
+        proof_reserve(phase_ws / 4 + add_lits + add_cls + 16);
         a.c = view();
         a.cls_scan = ve_cls_scan.p;
         a.lit_scan = ve_lit_scan.p;
@@ -1131,8 +1163,10 @@ struct pf_sigma_ctx {
 #endif
         kclock[K_BVEW].stop(rt);
         kbytes[K_BVEW] += phase_ws + 4ull * add_lits + 8ull * add_cls + 4ull * add_wit;
+        const u32 first_new = ncls;
         ncls += add_cls;
         nlits_used += add_lits;
+        proof_clauses(first_new);
         nresolved += add_wit;
         word_to(counters.p + 0, 0);
         read_slots_checked();
@@ -1176,6 +1210,7 @@ struct pf_sigma_ctx {
     // ERE (elimination.cpp:169-197).
     void ere() {
         if (!opt.ere || !npvs) return;
+        proof_reserve(nlits_used + ncls + 16);  // a deletion line per clause at most
         if (opt.ere_max > 65535) throw std::runtime_error("eremax above 65535 is not supported");
         EreArgs a;
         a.c = view();
@@ -2085,6 +2120,11 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     pf_sigma_ctx& c = *ctx;
     std::memset(&c.st, 0, sizeof(c.st));
     c.dump.clear();
+    c.proof_bound = 0;
+    if (c.opt.proof) {
+        c.rt.zero(c.counters64.p + 4, 8);
+        c.proof_reserve(2ull * c.nvars + 4096);  // every unit of the round: [1, lit]
+    }
     c.alg_bytes = 0;
     c.mis_rounds = 0;
     c.rt.launches = 0;
@@ -2110,6 +2150,7 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
         whole.start(c.rt);
         if (c.nf) {
             if (c.opt.dump_level > 0) throw std::runtime_error("round dumps are not written for formula batches");
+            if (c.opt.proof) throw std::runtime_error("proofs are recorded for single formulas only");
             c.round_batch();
         } else if (!(!o.phases && !(o.all || o.ere))) {
             c.round();
@@ -2251,6 +2292,53 @@ pf_status pf_sigma_batch_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* o
                 w += c.h_f_nv[f];
             }
         }
+        return PF_OK;
+    });
+}
+
+// One binary DRAT line (src/cpu/proof.cpp:95-135): 'a' or 'd', every literal in
+// 7-bit groups (low group first, high bit set on all but the last), a 0 byte.
+static void drat_line(std::vector<uint8_t>& out, char tag, const u32* lits, u32 n) {
+    out.push_back((uint8_t)tag);
+    for (u32 i = 0; i < n; i++) {
+        u32 r = lits[i];
+        while (r & ~127u) {
+            out.push_back((uint8_t)((r & 127u) | 128u));
+            r >>= 7;
+        }
+        out.push_back((uint8_t)r);
+    }
+    out.push_back(0);
+}
+
+pf_status pf_sigma_proof(pf_sigma_ctx* ctx, uint8_t* out, uint64_t* bytes) {
+    if (!ctx || !bytes) return fail("null argument", PF_EINVAL);
+    if (!ctx->opt.proof) return fail("the context records no proof (option proof = 0)", PF_ESTATE);
+    if (!ctx->rounds_run || (ctx->st.status != PF_OK && ctx->st.status != PF_UNSAT))
+        return fail("no finished round", PF_ESTATE);
+    return guarded([&]() -> pf_status {
+        pf_sigma_ctx& c = *ctx;
+        u64 words = 0;
+        c.rt.d2h(&words, c.counters64.p + 4, 8);
+        if (words > c.proof.n) throw std::runtime_error("proof buffer overflow");
+        std::vector<u32> w = c.fetch(c.proof.p, (size_t)words);
+        std::vector<uint8_t> enc;
+        enc.reserve((size_t)words * 3 + 8);
+        for (u64 i = 0; i < words;) {
+            const u32 n = w[i] & ~PROOF_DELETE;
+            if (i + 1 + n > words) throw std::runtime_error("malformed proof buffer");
+            drat_line(enc, (w[i] & PROOF_DELETE) ? 'd' : 'a', w.data() + i + 1, n);
+            i += 1 + n;
+        }
+        if (c.st.status == PF_UNSAT) drat_line(enc, 'a', nullptr, 0);
+        if (out) {
+            if (*bytes < enc.size()) {
+                *bytes = enc.size();
+                return fail("proof buffer too small", PF_EINVAL);
+            }
+            std::memcpy(out, enc.data(), enc.size());
+        }
+        *bytes = enc.size();
         return PF_OK;
     });
 }
@@ -2443,6 +2531,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     for (auto* b : b8) b->free();
     c.sub_units.free();
     c.sub_pairs.free();
+    c.proof.free();
     c.tm.destroy();
     for (auto& k : c.kclock) k.destroy();
     c.rt.destroy();

@@ -10,7 +10,7 @@ from __future__ import annotations
 import numpy as np
 
 KIND = {1: "cnf", 2: "otsize", 3: "scores", 4: "eligible", 5: "pvs", 6: "pvlists",
-        7: "trail", 8: "resolved", 9: "elim", 10: "counts", 11: "status", 12: "timing"}
+        7: "trail", 8: "resolved", 9: "elim", 10: "counts", 11: "status", 12: "timing", 13: "proofmark"}
 STAGE = {0: "input", 1: "prop", 2: "lcve", 3: "sort", 4: "sub", 5: "ve", 6: "bce", 7: "ere", 8: "final"}
 
 

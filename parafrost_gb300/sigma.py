@@ -86,6 +86,8 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     lib.pf_sigma_result_sizes.restype = ctypes.c_int
     lib.pf_sigma_download.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
     lib.pf_sigma_download.restype = ctypes.c_int
+    lib.pf_sigma_proof.argtypes = [_VP, _VP, _VP]
+    lib.pf_sigma_proof.restype = ctypes.c_int
     lib.pf_sigma_extend.argtypes = [_VP, _VP]
     lib.pf_sigma_extend.restype = ctypes.c_int
     lib.pf_sigma_write_dump.argtypes = [_VP, ctypes.c_char_p]
@@ -324,6 +326,14 @@ class Simplifier:
             out.append((int(st[f]), int(ph[f]), res))
             c0, u0, r0, e0 = c1, u1, r1, e1
         return out
+
+    def proof(self) -> bytes:
+        """The last round's DRAT proof (binary format); needs Options(proof=1)."""
+        n = _U64(0)
+        self._check(self.lib.pf_sigma_proof(self.h, None, ctypes.byref(n)))
+        buf = np.empty(max(n.value, 1), dtype=np.uint8)
+        self._check(self.lib.pf_sigma_proof(self.h, _ptr(buf), ctypes.byref(n)))
+        return buf[:n.value].tobytes()
 
     def extend(self, values: np.ndarray) -> np.ndarray:
         """MODEL::extend on the device for the single formula of the last round:

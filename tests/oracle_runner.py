@@ -35,6 +35,9 @@ def oracle_lib():
         _lib.oracle_sigmify.argtypes = [
             ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
             ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        _lib.oracle_check_drat.restype = ctypes.c_long
+        _lib.oracle_check_drat.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                           ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int)]
         _lib.oracle_extend_and_check.restype = ctypes.c_long
         _lib.oracle_extend_and_check.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
@@ -98,18 +101,27 @@ def reference_available() -> bool:
     return os.path.exists(REF_BIN)
 
 
-def run_reference(num_vars, lits, offsets, opts: Options | None = None, level: int = 2, learnt_tail: int = 0):
-    """Run the compiled reference round through its own DIMACS parser; returns records.
-    With learnt_tail, the last learnt_tail clauses enter the round as learnt clauses."""
+def run_reference(num_vars, lits, offsets, opts: Options | None = None, level: int = 2, learnt_tail: int = 0,
+                  proof: bool = False):
+    """Run the compiled reference round through its own DIMACS parser; returns records
+    (with proof, (records, the round's binary DRAT lines)). With learnt_tail, the last
+    learnt_tail clauses enter the round as learnt clauses."""
     opts = opts or Options(all=1)
     with tempfile.TemporaryDirectory() as td:
         cnf = os.path.join(td, "f.cnf")
         dump = os.path.join(td, "ref.dump")
+        prf = os.path.join(td, "ref.proof")
         cnfgen.to_dimacs(cnf, num_vars, lits, offsets)
         args = [REF_BIN, cnf, dump, str(level)] + ([f"--learnt-tail={learnt_tail}"] if learnt_tail else [])
-        args += opts.reference_flags()
+        args += opts.reference_flags() + (["-proof", f"--proofout={prf}"] if proof else [])
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
-        return rounddump.read(dump)
+        recs = rounddump.read(dump)
+        if not proof:
+            return recs
+        with open(prf, "rb") as f:
+            lines = drat_lines(f.read())
+        mark = [d for (k, ph, st, d) in recs if k == "proofmark"]
+        return recs, lines[int(mark[0][0]) if mark else 0:]
 
 
 def solver_available() -> bool:
@@ -145,3 +157,38 @@ def reference_solve(num_vars, lits, offsets, units=(), timeout: float = 600.0):
                 if x > 0:
                     model[x] = 1
     return "SAT", model
+
+
+def check_drat(num_vars, lits, offsets, proof: bytes):
+    """(first failing line or -1 when every addition is RUP, refutes) of a binary DRAT
+    proof against the formula (-2: malformed)."""
+    lits = np.ascontiguousarray(lits, dtype=np.uint32)
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+    buf = np.frombuffer(proof, dtype=np.uint8) if len(proof) else np.zeros(1, np.uint8)
+    empty = ctypes.c_int(0)
+    r = oracle_lib().oracle_check_drat(num_vars, lits.ctypes.data, offsets.ctypes.data, offsets.size - 1,
+                                       buf.ctypes.data, len(proof), ctypes.byref(empty))
+    return int(r), bool(empty.value)
+
+
+def drat_lines(proof: bytes) -> list:
+    """[(tag, (lit, ...))] of a binary DRAT proof."""
+    out, p, n = [], 0, len(proof)
+    while p < n:
+        tag = chr(proof[p])
+        p += 1
+        lits = []
+        while True:
+            r, shift = 0, 0
+            while True:
+                b = proof[p]
+                p += 1
+                r |= (b & 127) << shift
+                shift += 7
+                if not b & 128:
+                    break
+            if r == 0:
+                break
+            lits.append(r)
+        out.append((tag, tuple(lits)))
+    return out
