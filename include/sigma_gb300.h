@@ -83,7 +83,8 @@ typedef struct {
     uint64_t algorithmic_bytes; /* bytes the round's kernels must move (HBM roofline numerator) */
     uint32_t kernel_launches;   /* kernels launched by the round */
     uint32_t mis_rounds;        /* push/pull rounds of the independent-set elections */
-    uint32_t reserved[2];
+    uint32_t prop_waves;        /* waves of the in-round unit propagations */
+    uint32_t host_syncs;        /* times the host waited for the device during the round */
     /* The hottest kernels, timed with CUDA events on the context stream:
      * [0] independent-set rounds (LCVE), [1] BVE decision, [2] SUB, [3] BVE write. */
     double ms_kernel[4];        /* device time summed over the round's launches */

@@ -320,10 +320,6 @@ struct Round {
     // ParaFROST::LCVE (src/cpu/lcve.cpp:46-81).
     bool LCVE() {
         varReorder();
-        if (level >= 2) {
-            dump.rec(sigdump::K_SCORES, phase, sigdump::S_LCVE, scores);
-            dump.rec(sigdump::K_ELIGIBLE, phase, sigdump::S_LCVE, eligible);
-        }
         PVs.clear();
         const u32 pt = (u32)opts.mu_pos << mu_inc, nt = (u32)opts.mu_neg << mu_inc;
         for (u32 i = 0; i < eligible.size(); i++) {
@@ -339,7 +335,13 @@ struct Round {
             depFreeze(ot[n], cand, pt, nt);
         }
         std::fill(frozen.begin(), frozen.end(), 0);
-        return PVs.size() >= (size_t)opts.lcve_min;
+        const bool go = PVs.size() >= (size_t)opts.lcve_min;
+        // the reference harness records the order only for an election that goes on
+        if (go && level >= 2) {
+            dump.rec(sigdump::K_SCORES, phase, sigdump::S_LCVE, scores);
+            dump.rec(sigdump::K_ELIGIBLE, phase, sigdump::S_LCVE, eligible);
+        }
+        return go;
     }
 
     // ---------------------------------------------------------------- sortOT

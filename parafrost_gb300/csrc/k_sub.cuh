@@ -8,11 +8,16 @@
 // becomes a unit: the reference enqueues it and at once deletes every clause of
 // ot[unit] (elimination.cpp:214-226), which later variables then see deleted.
 // Units can only come from a binary (x u) next to a binary (-x u) at the start of
-// SUB; when no elected variable has such a pair the parallel pass is exact. When
-// one does, the driver checkpoints the lists, runs the pass, and re-runs (from the
-// checkpoint, with the earlier units' clauses pre-deleted) every variable that an
-// earlier variable's unit reaches, until nothing changes. Inside one variable the
-// reference's immediate deletion is applied to its own clauses.
+// SUB (SUB only removes x from a clause, and only deletes clauses otherwise); when
+// no elected variable has such a pair the parallel pass is exact. When some do
+// (the producers), the driver settles the producers first: it checkpoints their
+// lists, runs them, and re-runs (from the checkpoint, with the earlier producers'
+// units' clauses pre-deleted) every producer whose set of such units changed,
+// until none does. The other variables yield no unit, so one run of each, with the
+// units of the producers before it pre-deleted, is exact. Inside one variable the
+// reference's immediate deletion is applied to its own clauses. The bookkeeping
+// (which units reach which variable, sorted and compared per variable) runs on the
+// device.
 #pragma once
 
 #include "cnf.cuh"
@@ -238,11 +243,13 @@ HD void k_sub_pv(const SubArgs& a, u32 k) {
 }
 
 // Whether SUB on this variable can produce a unit: some binary (x u) in the
-// positive list next to a binary (-x u) in the negative list.
-HD void k_sub_unit_possible(const SubArgs& a, u32* flag, u32 k) {
+// positive list next to a binary (-x u) in the negative list. Counts producers in
+// *flag and, with prod, sets prod[k] (cleared first).
+HD void k_sub_unit_possible(const SubArgs& a, u32* flag, u32* prod, u32 k) {
     const Ctx& c = a.c;
     const u32 v = a.pvs[k];
     const u32 p = V2L(v), n = NEG(p);
+    if (prod) prod[k] = 0;
     if (c.ot_size[p] > a.sub_max || c.ot_size[n] > a.sub_max) return;
     const u32 po = c.ot_off[p], ps = c.ot_size[p], no = c.ot_off[n], ns = c.ot_size[n];
     for (u32 i = 0; i < ps; i++) {
@@ -255,7 +262,11 @@ HD void k_sub_unit_possible(const SubArgs& a, u32* flag, u32 k) {
             if (hj.size != 2 || h_deleted(hj.flags)) continue;
             const u32* lj = c.lits + hj.start;
             const u32 uj = lj[0] == n ? lj[1] : lj[0];
-            if (ui == uj) { atom_add(flag, 1u); return; }
+            if (ui == uj) {
+                atom_add(flag, 1u);
+                if (prod) prod[k] = 1;
+                return;
+            }
         }
     }
 }
@@ -275,7 +286,12 @@ struct SubCkptArgs {
     const uint8_t* run;   // restore only these (null = all)
 };
 
-HD void k_sub_need(const Ctx& c, const u32* pvs, u32* ent, u64* words, u32 k) {
+HD void k_sub_need(const Ctx& c, const u32* pvs, const uint8_t* only, u32* ent, u64* words, u32 k) {
+    if (only && !only[k]) {
+        ent[k] = 0;
+        words[k] = 0;
+        return;
+    }
     const u32 p = V2L(pvs[k]);
     u32 e = 0;
     u64 w = 0;
@@ -289,6 +305,7 @@ HD void k_sub_need(const Ctx& c, const u32* pvs, u32* ent, u64* words, u32 k) {
 }
 
 HD void k_sub_save(const SubCkptArgs& a, u32 k) {
+    if (a.run && !a.run[k]) return;
     const Ctx& c = a.c;
     const u32 p = V2L(a.pvs[k]);
     u32 e = a.ent_off[k];
@@ -336,6 +353,7 @@ struct SubReachArgs {
     U2* pairs;         // (target rank, unit index)
     u32* npairs;
     u32 cap_pairs;
+    const uint8_t* target;  // targets considered (per rank); null = all
 };
 // One item per (unit, clause of the unit's list): a unit's list can be long (hub
 // variables), so its clauses are spread over threads. item_off is the exclusive
@@ -355,6 +373,7 @@ HD void k_sub_reach(const SubReachArgs& a, const u32* item_off, u32 nunits, u32 
     for (u32 t = 0; t < h.size; t++) {
         const u32 owner = c.pvrank[ABS(l[t])];
         if (owner != NONE && owner > u.x) {
+            if (a.target && !a.target[owner]) break;
             const u32 pos = atom_add(a.npairs, 1u);
             if (pos < a.cap_pairs) a.pairs[pos] = mk_u2(owner, q);
             else set_err(c, ERR_CAP_SCRATCH);
@@ -363,6 +382,42 @@ HD void k_sub_reach(const SubReachArgs& a, const u32* item_off, u32 nunits, u32 
     }
 }
 HD void k_sub_reach_size(const Ctx& c, const U2* units, u32* size, u32 q) { size[q] = c.ot_size[units[q].y]; }
+
+// ---------------------------------------------------------------- unit sets
+// The units every variable must see pre-deleted: reach pairs (target rank, unit)
+// become the sorted set of distinct (rank, literal) pairs, segmented per rank; a
+// variable re-runs when its segment differs from the one its last run used.
+HD void k_subfx_pairlit(const U2* pairs, const U2* units, u32* rank, u32* lit, u32 i) {
+    rank[i] = pairs[i].x;
+    lit[i] = units[pairs[i].y].y;
+}
+HD void k_subfx_first(const u32* rank, const u32* lit, u32* flag, u32 i) {
+    flag[i] = (i == 0 || rank[i] != rank[i - 1] || lit[i] != lit[i - 1]) ? 1u : 0u;
+}
+HD void k_subfx_scatter(const u32* rank, const u32* lit, const u32* flag, const u32* scan, u32* orank, u32* olit,
+                        u32* count, u32 i) {
+    if (!flag[i]) return;
+    orank[scan[i]] = rank[i];
+    olit[scan[i]] = lit[i];
+    atom_add(&count[rank[i]], 1u);
+}
+HD void k_subfx_diff(const u32* woff, const u32* wlit, const u32* uoff, const u32* ulit, const uint8_t* cand,
+                     u32* flag, uint8_t* run, u32 k) {
+    bool d = false;
+    if (cand[k]) {
+        const u32 a0 = woff[k], n = woff[k + 1] - a0, b0 = uoff[k];
+        d = n != uoff[k + 1] - b0;
+        for (u32 i = 0; !d && i < n; i++) d = wlit[a0 + i] != ulit[b0 + i];
+    }
+    flag[k] = d ? 1u : 0u;
+    run[k] = d ? 1 : 0;
+}
+// units of the variables that do not re-run stay
+HD void k_subfx_keep(const U2* units, const uint8_t* run, u32* flag, u32 i) { flag[i] = run[units[i].x] ? 0u : 1u; }
+HD void k_subfx_keep_scatter(const U2* units, const u32* flag, const u32* scan, U2* out, u32 i) {
+    if (flag[i]) out[scan[i]] = units[i];
+}
+HD void k_subfx_to8(const u32* f, uint8_t* b, bool invert, u32 k) { b[k] = (f[k] != 0) != invert ? 1 : 0; }
 
 // Commit of one unit: delete every clause of ot[lit] and empty the list.
 HD void k_sub_commit_oblivion(const Ctx& c, const u32* lits_, u32 q) {

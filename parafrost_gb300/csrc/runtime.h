@@ -72,6 +72,7 @@ struct Runtime {
     size_t bytes_live = 0;
     size_t budget = 0;  // 0 = no limit
     unsigned launches = 0;
+    unsigned syncs = 0;  // host waits for the device (synchronous reads, stream and event syncs)
 
     void init() {
 #if SIGMA_CUDA
@@ -132,6 +133,7 @@ struct Runtime {
     }
     void d2h(void* h, const void* d, size_t b) {
         if (!b) return;
+        syncs++;
 #if SIGMA_CUDA
         ck(cudaMemcpyAsync(h, d, b, cudaMemcpyDeviceToHost, stream), "d2h");
         ck(cudaStreamSynchronize(stream), "sync");
@@ -156,6 +158,7 @@ struct Runtime {
 #endif
     }
     void sync() {
+        syncs++;
 #if SIGMA_CUDA
         ck(cudaStreamSynchronize(stream), "sync");
 #endif
@@ -329,6 +332,7 @@ struct StageTimer {
 #endif
     }
     double stop(Runtime& rt) {
+        rt.syncs++;
 #if SIGMA_CUDA
         cudaEventRecord(b, rt.stream);
         cudaEventSynchronize(b);

@@ -69,9 +69,31 @@ struct FProofClause {
     }
 };
 struct FSortList { SortArgs a; HD void operator()(u32 i) const { k_sort_list(a, i); } };
-struct FSubPossible { SubArgs a; u32* flag; HD void operator()(u32 i) const { k_sub_unit_possible(a, flag, i); } };
+struct FSubPossible { SubArgs a; u32* flag; u32* prod; HD void operator()(u32 i) const { k_sub_unit_possible(a, flag, prod, i); } };
 struct FSubPv { SubArgs a; HD void operator()(u32 i) const { k_sub_pv(a, i); } };
-struct FSubNeed { Ctx c; const u32* pvs; u32* ent; u64* words; HD void operator()(u32 i) const { k_sub_need(c, pvs, ent, words, i); } };
+struct FSubNeed {
+    Ctx c; const u32* pvs; const uint8_t* only; u32* ent; u64* words;
+    HD void operator()(u32 i) const { k_sub_need(c, pvs, only, ent, words, i); }
+};
+struct FSubfxPairLit {
+    const U2* pairs; const U2* units; u32* rank; u32* lit;
+    HD void operator()(u32 i) const { k_subfx_pairlit(pairs, units, rank, lit, i); }
+};
+struct FSubfxFirst { const u32* rank; const u32* lit; u32* flag; HD void operator()(u32 i) const { k_subfx_first(rank, lit, flag, i); } };
+struct FSubfxScatter {
+    const u32* rank; const u32* lit; const u32* flag; const u32* scan; u32* orank; u32* olit; u32* count;
+    HD void operator()(u32 i) const { k_subfx_scatter(rank, lit, flag, scan, orank, olit, count, i); }
+};
+struct FSubfxDiff {
+    const u32* woff; const u32* wlit; const u32* uoff; const u32* ulit; const uint8_t* cand; u32* flag; uint8_t* run;
+    HD void operator()(u32 k) const { k_subfx_diff(woff, wlit, uoff, ulit, cand, flag, run, k); }
+};
+struct FSubfxKeep { const U2* units; const uint8_t* run; u32* flag; HD void operator()(u32 i) const { k_subfx_keep(units, run, flag, i); } };
+struct FSubfxKeepScatter {
+    const U2* units; const u32* flag; const u32* scan; U2* out;
+    HD void operator()(u32 i) const { k_subfx_keep_scatter(units, flag, scan, out, i); }
+};
+struct FSubfxTo8 { const u32* f; uint8_t* b; bool invert; HD void operator()(u32 k) const { k_subfx_to8(f, b, invert, k); } };
 struct FSubSave { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_save(a, i); } };
 struct FSubRestore { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_restore(a, i); } };
 struct FSubReach { SubReachArgs a; const u32* off; u32 nq; HD void operator()(u32 i) const { k_sub_reach(a, off, nq, i); } };
@@ -315,6 +337,11 @@ struct pf_sigma_ctx {
     DBuf<u64> sub_wrd, sub_wrd_off;
     DBuf<Hdr> sub_hdrs;
     DBuf<uint8_t> sub_run;
+    // SUB unit fix-point (device bookkeeping)
+    DBuf<u32> fx_prod, fx_rank, fx_lit, fx_k2, fx_v2, fx_flag, fx_scan;
+    DBuf<u32> want_rank, want_lit, want_cnt, want_off, used_lit, used_off;
+    DBuf<uint8_t> fx_prod8, fx_other8;
+    DBuf<U2> sub_units2;
     // ERE
     DBuf<u64> ere_claim, ere_key;
     DBuf<u32> ere_target, ere_losers;
@@ -345,6 +372,7 @@ struct pf_sigma_ctx {
     u64 kbytes[K_COUNT] = {};
     u64 phase_ws = 0;  // elected lists' working set of the current phase
     u32 mis_rounds = 0;
+    u32 prop_waves = 0;
 
     Ctx view() {
         Ctx c;
@@ -733,7 +761,9 @@ struct pf_sigma_ctx {
                                            rt.stream),
                "cooperative launch");
             check();
-            wave_stamp += read_u32(counters.p + 26);
+            const u32 waves = read_u32(counters.p + 26);
+            wave_stamp += waves;
+            prop_waves += waves;
             ntrail = read_u32(counters.p + 0);
             prop_head = ntrail;
         }
@@ -741,6 +771,7 @@ struct pf_sigma_ctx {
         u32 guard = 0;
         while (prop_head < ntrail) {
             if (++guard > loop_bound()) throw int(PF_ETIMEOUT);
+            prop_waves++;
             const u32 pend = ntrail - prop_head;
             PropArgs a;
             a.c = view();
@@ -873,12 +904,14 @@ struct pf_sigma_ctx {
         perm_off = 0;
         perm_n = npvs;
         alg_bytes += 4ull * D + 24ull * nvars;
-        if (opt.dump_level >= 2) {
+        const bool go = npvs >= (u32)opt.lcve_min;
+        // stage dumps record an election that goes on (as the reference harness does)
+        if (go && opt.dump_level >= 2) {
             rec(3, phase, 2, fetch(score.p, nvars + 1));
             rec(4, phase, 2, fetch(order.p, nvars));
         }
-        if (opt.dump_level >= 1) rec(5, phase, 2, fetch(pvs.p, npvs));
-        return npvs >= (u32)opt.lcve_min;
+        if (go && opt.dump_level >= 1) rec(5, phase, 2, fetch(pvs.p, npvs));
+        return go;
     }
 
     void sort_ot() {
@@ -934,7 +967,8 @@ struct pf_sigma_ctx {
         a.pre_lits = nullptr;
         a.run = nullptr;
         write_u32(counters.p + 5, 0);
-        rt.each(FSubPossible{a, counters.p + 5}, npvs);
+        fx_prod.reserve(rt, npvs + 1);
+        rt.each(FSubPossible{a, counters.p + 5, fx_prod.p}, npvs);
         kbytes[K_SUB] += phase_ws;
         if (read_u32(counters.p + 5) == 0) {
             kclock[K_SUB].start(rt);
@@ -949,123 +983,161 @@ struct pf_sigma_ctx {
         sub_safe(a);
     }
 
+    // Bits a radix key needs for values below n (multiples of 8).
+    static int key_bits(u64 n) {
+        int b = 8;
+        while (b < 32 && (n >> b)) b += 8;
+        return b;
+    }
+
+    // The sorted sets of unit literals (sub_units[0, nu)) that reach every target
+    // variable from an earlier one: want_off (npvs + 1 segment starts, by rank) and
+    // want_lit.
+    void sub_unit_sets(u32 nu, const uint8_t* target) {
+        want_cnt.reserve(rt, npvs + 1);
+        want_off.reserve(rt, npvs + 1);
+        rt.zero(want_cnt.p, ((size_t)npvs + 1) * 4);
+        u32 nwant = 0;
+        if (nu) {
+            big32a.reserve(rt, (size_t)nu + 1);
+            big32b.reserve(rt, (size_t)nu + 1);
+            rt.each(FSubReachSize{view(), sub_units.p, big32a.p}, nu);
+            const u32 items = scan32(big32a.p, big32b.p, nu);
+            sub_pairs.reserve(rt, (size_t)items + 16);
+            write_u32(counters.p + 6, 0);
+            SubReachArgs ra{view(), sub_units.p, sub_pairs.p, counters.p + 6, (u32)sub_pairs.n, target};
+            if (items) rt.each(FSubReach{ra, big32b.p, nu}, items);
+            const u32 np = read_u32(counters.p + 6);
+            if (np) {
+                fx_rank.reserve(rt, (size_t)np + 1);
+                fx_lit.reserve(rt, (size_t)np + 1);
+                fx_k2.reserve(rt, (size_t)np + 1);
+                fx_v2.reserve(rt, (size_t)np + 1);
+                fx_flag.reserve(rt, (size_t)np + 1);
+                fx_scan.reserve(rt, (size_t)np + 1);
+                rt.each(FSubfxPairLit{sub_pairs.p, sub_units.p, fx_rank.p, fx_lit.p}, np);
+                radix_hist.reserve(rt, radix_hist_elems(np));
+                radix_hscan.reserve(rt, radix_hist_elems(np));
+                scan_tmp32.reserve(rt, scan_tmp_elems(radix_hist_elems(np)) + 4);
+                // by literal, then stable by rank: (rank, literal) order
+                const int lb = key_bits(D), rb = key_bits(npvs);
+                radix_sort_pairs(fx_lit.p, fx_rank.p, fx_k2.p, fx_v2.p, np, lb, radix_hist.p, radix_hscan.p,
+                                 scan_tmp32.p, rt.stream);
+                radix_sort_pairs(fx_rank.p, fx_lit.p, fx_k2.p, fx_v2.p, np, rb, radix_hist.p, radix_hscan.p,
+                                 scan_tmp32.p, rt.stream);
+                rt.launches += 5 * (lb / 8 + rb / 8);
+                rt.each(FSubfxFirst{fx_rank.p, fx_lit.p, fx_flag.p}, np);
+                nwant = scan32(fx_flag.p, fx_scan.p, np);
+                want_rank.reserve(rt, (size_t)nwant + 1);
+                want_lit.reserve(rt, (size_t)nwant + 1);
+                rt.each(FSubfxScatter{fx_rank.p, fx_lit.p, fx_flag.p, fx_scan.p, want_rank.p, want_lit.p, want_cnt.p}, np);
+            }
+        }
+        want_lit.reserve(rt, (size_t)nwant + 1);
+        write_u32(want_off.p + npvs, scan32(want_cnt.p, want_off.p, npvs));
+    }
+
+    // SUB when units are possible (see k_sub.cuh): the producers settle by re-runs
+    // from their checkpoint, then every other variable runs once with the
+    // producers' units pre-deleted.
     void sub_safe(SubArgs a) {
         Ctx c = view();
-        // checkpoint
+        fx_prod8.reserve(rt, npvs + 1);
+        fx_other8.reserve(rt, npvs + 1);
+        sub_run.reserve(rt, npvs + 1);
+        rt.each(FSubfxTo8{fx_prod.p, fx_prod8.p, false}, npvs);
+        rt.each(FSubfxTo8{fx_prod.p, fx_other8.p, true}, npvs);
+        // checkpoint of the producers
         sub_ent.reserve(rt, npvs + 1);
         sub_ent_off.reserve(rt, npvs + 1);
         sub_wrd.reserve(rt, npvs + 1);
         sub_wrd_off.reserve(rt, npvs + 1);
-        rt.each(FSubNeed{c, pvs.p, sub_ent.p, sub_wrd.p}, npvs);
+        rt.each(FSubNeed{c, pvs.p, fx_prod8.p, sub_ent.p, sub_wrd.p}, npvs);
         const u32 ents = scan32(sub_ent.p, sub_ent_off.p, npvs);
         const u64 words = scan64(sub_wrd.p, sub_wrd_off.p, npvs);
         sub_ids.reserve(rt, ents + 1);
         sub_hdrs.reserve(rt, ents + 1);
         sub_words.reserve(rt, (size_t)words + 1);
         sub_sizes.reserve(rt, 2 * npvs + 2);
-        SubCkptArgs ck{c, pvs.p, sub_ent_off.p, sub_wrd_off.p, sub_ids.p, sub_hdrs.p, sub_words.p, sub_sizes.p, nullptr};
+        SubCkptArgs ck{c, pvs.p, sub_ent_off.p, sub_wrd_off.p, sub_ids.p, sub_hdrs.p, sub_words.p, sub_sizes.p,
+                       fx_prod8.p};
         rt.each(FSubSave{ck}, npvs);
-        // first pass
+        // the producers' first run
         sub_units.reserve(rt, (size_t)ents + 16);
+        sub_units2.reserve(rt, sub_units.n);
         a.units = sub_units.p;
         a.cap_units = (u32)sub_units.n;
+        a.run = fx_prod8.p;
         write_u32(counters.p + 4, 0);
         kclock[K_SUB].start(rt);
         sub_pass(a);
         kclock[K_SUB].stop(rt);
         check();
         u32 nu = read_u32(counters.p + 4);
-        if (nu == 0) return;
-        // host bookkeeping: units per producer, used pre-deletions per PV
-        std::vector<U2> units = fetch(sub_units.p, nu);
-        std::map<u32, std::vector<u32>> used;  // PV rank -> literals pre-deleted in its last run
-        sub_run.reserve(rt, npvs);
-        for (int iter = 0;; iter++) {
-            if (iter > (int)npvs + 2) throw int(PF_ETIMEOUT);
-            // reach pairs from the current units
-            std::sort(units.begin(), units.end(), [](const U2& x, const U2& y) { return x.x < y.x; });
-            sub_ulits.reserve(rt, units.size() + 1);
-            sub_units.reserve(rt, std::max<size_t>(units.size(), 16));
-            rt.h2d(sub_units.p, units.data(), units.size() * sizeof(U2));
-            const size_t cap_pairs = 1 << 20;
-            sub_pairs.reserve(rt, cap_pairs);
-            write_u32(counters.p + 6, 0);
-            SubReachArgs ra{view(), sub_units.p, sub_pairs.p, counters.p + 6, (u32)cap_pairs};
-            const u32 nq = (u32)units.size();
-            big32a.reserve(rt, (size_t)nq + 1);
-            big32b.reserve(rt, (size_t)nq + 1);
-            rt.each(FSubReachSize{view(), sub_units.p, big32a.p}, nq);
-            const u32 items = scan32(big32a.p, big32b.p, nq);
-            rt.each(FSubReach{ra, big32b.p, nq}, items);
-            check();
-            const u32 np = read_u32(counters.p + 6);
-            std::vector<U2> pairs = fetch(sub_pairs.p, np);
-            std::map<u32, std::vector<u32>> want;
-            for (const U2& pr : pairs) want[pr.x].push_back(units[pr.y].y);
-            for (auto& kv : want) {
-                std::sort(kv.second.begin(), kv.second.end());
-                kv.second.erase(std::unique(kv.second.begin(), kv.second.end()), kv.second.end());
-            }
-            // PVs whose pre-deleted set changed
-            std::vector<u32> rerun;
-            std::set<u32> keys;
-            for (auto& kv : want) keys.insert(kv.first);
-            for (auto& kv : used) keys.insert(kv.first);
-            for (u32 k : keys) {
-                const auto w = want.count(k) ? want[k] : std::vector<u32>();
-                const auto u = used.count(k) ? used[k] : std::vector<u32>();
-                if (w != u) rerun.push_back(k);
-            }
-            if (rerun.empty()) break;
-            // restore and re-run them with their pre-deletions
-            std::vector<uint8_t> run(npvs, 0);
-            for (u32 k : rerun) run[k] = 1;
-            rt.h2d(sub_run.p, run.data(), npvs);
+        // fix-point among the producers: a producer re-runs when the set of earlier
+        // producers' units that reach it differs from the set its last run used
+        used_off.reserve(rt, npvs + 1);
+        used_lit.reserve(rt, 1);
+        rt.zero(used_off.p, ((size_t)npvs + 1) * 4);
+        fx_flag.reserve(rt, npvs + 1);
+        fx_scan.reserve(rt, npvs + 1);
+        for (u32 iter = 0;; iter++) {
+            if (iter > npvs + 2) throw int(PF_ETIMEOUT);
+            sub_unit_sets(nu, fx_prod8.p);
+            fx_flag.reserve(rt, npvs + 1);
+            fx_scan.reserve(rt, npvs + 1);
+            rt.each(FSubfxDiff{want_off.p, want_lit.p, used_off.p, used_lit.p, fx_prod8.p, fx_flag.p, sub_run.p}, npvs);
+            const u32 nrerun = scan32(fx_flag.p, fx_scan.p, npvs);
+            if (!nrerun) break;
+            // restore the re-runs; they use the new sets
             SubCkptArgs rk = ck;
             rk.c = view();
             rk.run = sub_run.p;
             rt.each(FSubRestore{rk}, npvs);
-            std::vector<u32> poff(npvs + 1, 0), plits;
-            for (u32 k = 0; k < npvs; k++) {
-                poff[k] = (u32)plits.size();
-                if (run[k] && want.count(k)) plits.insert(plits.end(), want[k].begin(), want[k].end());
+            std::swap(used_lit, want_lit);
+            std::swap(used_off, want_off);
+            // their old units go, the others' stay
+            fx_flag.reserve(rt, (size_t)nu + 1);
+            fx_scan.reserve(rt, (size_t)nu + 1);
+            u32 nkeep = 0;
+            if (nu) {
+                rt.each(FSubfxKeep{sub_units.p, sub_run.p, fx_flag.p}, nu);
+                nkeep = scan32(fx_flag.p, fx_scan.p, nu);
+                rt.each(FSubfxKeepScatter{sub_units.p, fx_flag.p, fx_scan.p, sub_units2.p}, nu);
+                std::swap(sub_units, sub_units2);
             }
-            poff[npvs] = (u32)plits.size();
-            sub_pre_off.reserve(rt, npvs + 1);
-            sub_pre_lits.reserve(rt, plits.size() + 1);
-            rt.h2d(sub_pre_off.p, poff.data(), poff.size() * 4);
-            rt.h2d(sub_pre_lits.p, plits.data(), plits.size() * 4);
-            for (u32 k : rerun) {
-                if (want.count(k)) used[k] = want[k];
-                else used.erase(k);
-            }
-            // drop the re-run PVs' old units, collect their new ones
-            std::vector<U2> kept;
-            for (const U2& u : units) if (!run[u.x]) kept.push_back(u);
-            sub_units.reserve(rt, (size_t)ents + 16);
             SubArgs b = a;
             b.c = view();
             b.units = sub_units.p;
             b.cap_units = (u32)sub_units.n;
-            b.pre_off = sub_pre_off.p;
-            b.pre_lits = sub_pre_lits.p;
+            b.pre_off = used_off.p;
+            b.pre_lits = used_lit.p;
             b.run = sub_run.p;
-            write_u32(counters.p + 4, 0);
+            write_u32(counters.p + 4, nkeep);
             sub_pass(b);
             check();
-            const u32 nn = read_u32(counters.p + 4);
-            std::vector<U2> fresh = fetch(sub_units.p, nn);
-            kept.insert(kept.end(), fresh.begin(), fresh.end());
-            units.swap(kept);
+            nu = read_u32(counters.p + 4);
         }
+        // every other variable once, with the units of the producers before it pre-deleted
+        sub_unit_sets(nu, fx_other8.p);
+        SubArgs b = a;
+        b.c = view();
+        b.units = sub_units.p;
+        b.cap_units = (u32)sub_units.n;
+        b.pre_off = want_off.p;
+        b.pre_lits = want_lit.p;
+        b.run = fx_other8.p;
+        write_u32(counters.p + 4, nu);
+        sub_pass(b);
+        check();
+        nu = read_u32(counters.p + 4);
         // commit: enqueueUnit + toblivion(ot[unit]). The reference commits in producer
         // order; the outcome does not depend on it (the same literals end assigned, an
         // opposite pair is a conflict either way), so the units go to the trail in
         // parallel, first claim wins, and the newly assigned ones empty their lists.
-        sub_units.reserve(rt, std::max<size_t>(units.size(), 16));
-        rt.h2d(sub_units.p, units.data(), units.size() * sizeof(U2));
+        if (!nu) return;
         const u32 before = ntrail;
-        rt.each(FSubAssign{view(), sub_units.p}, (u32)units.size());
+        rt.each(FSubAssign{view(), sub_units.p}, nu);
         ntrail = read_u32(counters.p + 0);
         if (ntrail > before) rt.each(FSubCommit{view(), trail.p + before}, ntrail - before);
         check();
@@ -2127,7 +2199,9 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     }
     c.alg_bytes = 0;
     c.mis_rounds = 0;
+    c.prop_waves = 0;
     c.rt.launches = 0;
+    c.rt.syncs = 0;
     c.compact = false;
     for (int k = 0; k < pf_sigma_ctx::K_COUNT; k++) {
         c.kclock[k].reset();
@@ -2182,6 +2256,8 @@ pf_status pf_sigma_round(pf_sigma_ctx* ctx, pf_round_stats* stats) {
     c.st.algorithmic_bytes = c.alg_bytes;
     c.st.kernel_launches = c.rt.launches;
     c.st.mis_rounds = c.mis_rounds;
+    c.st.prop_waves = c.prop_waves;
+    c.st.host_syncs = c.rt.syncs;
     if (status == PF_OK || status == PF_UNSAT) {
         try {
             c.rt.sync();
@@ -2530,7 +2606,13 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     c.pv_key.free();
     for (auto* b : b8) b->free();
     c.sub_units.free();
+    c.sub_units2.free();
     c.sub_pairs.free();
+    DBuf<u32>* fx[] = {&c.fx_prod, &c.fx_rank, &c.fx_lit, &c.fx_k2, &c.fx_v2, &c.fx_flag, &c.fx_scan, &c.want_rank,
+                       &c.want_lit, &c.want_cnt, &c.want_off, &c.used_lit, &c.used_off};
+    for (auto* b : fx) b->free();
+    c.fx_prod8.free();
+    c.fx_other8.free();
     c.proof.free();
     c.tm.destroy();
     for (auto& k : c.kclock) k.destroy();

@@ -46,7 +46,7 @@ class RoundStats(ctypes.Structure):
                 ("resolved_words", ctypes.c_uint64), ("ms_total", ctypes.c_double),
                 ("ms_stage", ctypes.c_double * 12), ("algorithmic_bytes", ctypes.c_uint64),
                 ("kernel_launches", ctypes.c_uint32), ("mis_rounds", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 2), ("ms_kernel", ctypes.c_double * 4),
+                ("prop_waves", ctypes.c_uint32), ("host_syncs", ctypes.c_uint32), ("ms_kernel", ctypes.c_double * 4),
                 ("bytes_kernel", ctypes.c_uint64 * 4), ("launches_kernel", ctypes.c_uint32 * 4),
                 ("phase_elected", ctypes.c_uint32 * 8), ("phase_clauses", ctypes.c_uint64 * 8),
                 ("phase_literals", ctypes.c_uint64 * 8), ("phase_bytes", ctypes.c_uint64 * 8),
@@ -56,7 +56,7 @@ class RoundStats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_
-             if f not in ("ms_stage", "reserved", "ms_kernel", "bytes_kernel", "launches_kernel")
+             if f not in ("ms_stage", "ms_kernel", "bytes_kernel", "launches_kernel")
              and f not in self.PHASE_FIELDS}
         d["ms_stage"] = {s: self.ms_stage[i] for i, s in enumerate(STAGES)}
         d["kernels"] = {k: {"ms": self.ms_kernel[i], "bytes": int(self.bytes_kernel[i]),

@@ -55,3 +55,24 @@ def test_emu_stagewise(built, case, seed, opt):
     stats, b, _ = run_lib(build.EMU, nv, lits, off, opts, level=2)
     assert stats.status == st
     assert rd.compare(rd.normalize(a), rd.normalize(b)) == []
+
+
+# Formulas whose SUB pass finds units in a variable that an earlier variable's unit
+# reaches, so the producers' fix-point re-runs some of them (the rare path).
+SUB_RERUN = [
+    ("ksat2_60_s5", lambda: cnfgen.random_ksat(60, 75, 2, seed=5)),
+    ("ksat2_60_s36", lambda: cnfgen.random_ksat(60, 106, 2, seed=36)),
+    ("ksat2_150_s63", lambda: cnfgen.random_ksat(150, 213, 2, seed=63)),
+    ("ksat2_150_s161", lambda: cnfgen.random_ksat(150, 311, 2, seed=161)),
+]
+
+
+@pytest.mark.parametrize("case", [c[0] for c in SUB_RERUN])
+@pytest.mark.parametrize("opt", [dict(all=1, mu_pos=10, mu_neg=10), dict(all=1)])
+def test_emu_sub_rerun(built, case, opt):
+    nv, lits, off = dict(SUB_RERUN)[case]()
+    opts = Options(**opt)
+    st, a, _ = orr.run_oracle(nv, lits, off, opts, level=2)
+    stats, b, _ = run_lib(build.EMU, nv, lits, off, opts, level=2)
+    assert stats.status == st
+    assert rd.compare(rd.normalize(a), rd.normalize(b)) == []

@@ -8,7 +8,7 @@ import oracle_runner as orr
 from parafrost_gb300 import build, cnfgen, rounddump as rd
 from parafrost_gb300.options import Options
 from parafrost_gb300.sigma import PF_EINVAL, PF_ESTATE, SigmaError, Simplifier
-from test_emu import CASES, run_lib
+from test_emu import CASES, SUB_RERUN, run_lib
 
 pytestmark = pytest.mark.gpu
 
@@ -74,3 +74,15 @@ def test_gpu_invalid_input(cuda_lib):
         with pytest.raises(SigmaError) as e:
             s.awaken(3, oob, np.array([0, 2], dtype=np.uint64))
         assert e.value.status == PF_EINVAL
+
+
+@pytest.mark.parametrize("case", [c[0] for c in SUB_RERUN])
+@pytest.mark.parametrize("opt", [dict(all=1, mu_pos=10, mu_neg=10), dict(all=1)])
+def test_gpu_sub_rerun(cuda_lib, built, case, opt):
+    """The SUB units' fix-point with re-runs, stage by stage against the oracle."""
+    nv, lits, off = dict(SUB_RERUN)[case]()
+    opts = Options(**opt)
+    st, a, _ = orr.run_oracle(nv, lits, off, opts, level=2)
+    stats, b, _ = run_lib(cuda_lib, nv, lits, off, opts, level=2)
+    assert stats.status == st
+    assert rd.compare(rd.normalize(a), rd.normalize(b)) == []
