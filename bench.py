@@ -42,6 +42,9 @@ WORKLOADS = {
                      sample_kw=dict(num_inputs=50_000, num_and=2_000_000, num_xor=200_000, seed=1)),
     "community-20m": dict(gen="community", kw=dict(seed=1),
                           sample_kw=dict(num_vars=2_000_000, num_clauses=8_000_000, seed=1)),
+    # the same generator at a tenth of the size (profiling captures)
+    "community-2m": dict(gen="community", kw=dict(num_vars=2_000_000, num_clauses=8_000_000, seed=1),
+                         sample_kw=dict(num_vars=2_000_000, num_clauses=8_000_000, seed=1)),
     "ksat3-10k": dict(gen="random_ksat", kw=dict(num_vars=10_000, num_clauses=42_600, k=3, seed=1),
                       sample_kw=dict(num_vars=10_000, num_clauses=42_600, k=3, seed=1)),
     # batched workload: 4096 random k-SAT formulas (k in 2..5 per clause), clause counts

@@ -419,12 +419,20 @@ HD void k_subfx_keep_scatter(const U2* units, const u32* flag, const u32* scan, 
 }
 HD void k_subfx_to8(const u32* f, uint8_t* b, bool invert, u32 k) { b[k] = (f[k] != 0) != invert ? 1 : 0; }
 
-// Commit of one unit: delete every clause of ot[lit] and empty the list.
-HD void k_sub_commit_oblivion(const Ctx& c, const u32* lits_, u32 q) {
-    const u32 lit = lits_[q];
-    const u32 o = c.ot_off[lit], s = c.ot_size[lit];
-    for (u32 i = 0; i < s; i++) mark_deleted(c, c.ot_refs[o + i]);
-    c.ot_size[lit] = 0;
+// Commit of the units, spread over the clauses of their lists (a hub literal's
+// list is long): item i is clause i - item_off[q] of ot[lits[q]]; the lists are
+// emptied afterwards (k_sub_commit_clear).
+HD void k_sub_commit_size(const Ctx& c, const u32* lits_, u32* size, u32 q) { size[q] = c.ot_size[lits_[q]]; }
+HD void k_sub_commit_item(const Ctx& c, const u32* lits_, const u32* item_off, u32 nunits, u32 item) {
+    u32 lo = 0, hi = nunits;
+    while (hi - lo > 1) {
+        const u32 mid = (lo + hi) >> 1;
+        if (item_off[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    const u32 lit = lits_[lo];
+    mark_deleted(c, c.ot_refs[c.ot_off[lit] + (item - item_off[lo])]);
 }
+HD void k_sub_commit_clear(const Ctx& c, const u32* lits_, u32 q) { c.ot_size[lits_[q]] = 0; }
 
 }  // namespace sigma

@@ -99,7 +99,12 @@ struct FSubRestore { SubCkptArgs a; HD void operator()(u32 i) const { k_sub_rest
 struct FSubReach { SubReachArgs a; const u32* off; u32 nq; HD void operator()(u32 i) const { k_sub_reach(a, off, nq, i); } };
 struct FSubReachSize { Ctx c; const U2* units; u32* size; HD void operator()(u32 q) const { k_sub_reach_size(c, units, size, q); } };
 struct FSubWarp { SubArgs a; HD void operator()(u32 k) const { sub_warp_pv(a, k); } };
-struct FSubCommit { Ctx c; const u32* lits; HD void operator()(u32 i) const { k_sub_commit_oblivion(c, lits, i); } };
+struct FSubCommitSize { Ctx c; const u32* lits; u32* size; HD void operator()(u32 q) const { k_sub_commit_size(c, lits, size, q); } };
+struct FSubCommitItem {
+    Ctx c; const u32* lits; const u32* off; u32 n;
+    HD void operator()(u32 i) const { k_sub_commit_item(c, lits, off, n, i); }
+};
+struct FSubCommitClear { Ctx c; const u32* lits; HD void operator()(u32 q) const { k_sub_commit_clear(c, lits, q); } };
 struct FSubAssign { Ctx c; const U2* units; HD void operator()(u32 i) const { enqueue_unit(c, units[i].y); } };
 struct FBveNeed { Ctx c; const u32* pvs; u64* need; HD void operator()(u32 i) const { k_bve_scratch_need(c, pvs, need, i); } };
 struct FBveWarp { BveArgs a; HD void operator()(u32 i) const { k_bve_warp(a, i); } };
@@ -111,6 +116,20 @@ struct FEreCount { EreArgs a; const u32* perm; u64* cnt; HD void operator()(u32 
 struct FErePair { EreArgs a; const u32* perm; const u64* off; u32 n; HD void operator()(u32 i) const { k_ere_pair(a, perm, off, n, i); } };
 struct FEreResolve { EreArgs a; HD void operator()(u32 i) const { k_ere_resolve(a, i); } };
 struct FEreFix { EreArgs a; const u64* keys; u32 n; HD void operator()() const { ere_fixup(a, keys, n); } };
+// Sort keys of the ERE losers: loser order[i]'s low key word (hi = false; order[i] =
+// i set first) or high key word (hi = true), and the keys in sorted order.
+struct FEreLoserKey {
+    const u64* key; const u32* losers; u32* order; u32* out; bool hi;
+    HD void operator()(u32 i) const {
+        if (!hi) order[i] = i;
+        const u64 k = key[losers[order[i]]];
+        out[i] = hi ? (u32)(k >> 32) : (u32)k;
+    }
+};
+struct FEreLoserGather {
+    const u64* key; const u32* losers; const u32* order; u64* out;
+    HD void operator()(u32 i) const { out[i] = key[losers[order[i]]]; }
+};
 struct FEreSeq { EreArgs a; HD void operator()() const { ere_sequential(a); } };
 // Item i of a permuted launch runs f(perm[i]).
 template <class F>
@@ -1139,7 +1158,16 @@ struct pf_sigma_ctx {
         const u32 before = ntrail;
         rt.each(FSubAssign{view(), sub_units.p}, nu);
         ntrail = read_u32(counters.p + 0);
-        if (ntrail > before) rt.each(FSubCommit{view(), trail.p + before}, ntrail - before);
+        if (ntrail > before) {
+            const u32 na = ntrail - before;
+            const u32* ul = trail.p + before;
+            big32a.reserve(rt, (size_t)na + 1);
+            big32b.reserve(rt, (size_t)na + 1);
+            rt.each(FSubCommitSize{view(), ul, big32a.p}, na);
+            const u32 items = scan32(big32a.p, big32b.p, na);
+            if (items) rt.each(FSubCommitItem{view(), ul, big32b.p, na}, items);
+            rt.each(FSubCommitClear{view(), ul}, na);
+        }
         check();
     }
 
@@ -1322,15 +1350,25 @@ struct pf_sigma_ctx {
         rt.each(FEreResolve{a}, nrec);
         const u32 nl = read_u32(counters.p + 8);
         if (nl) {
-            std::vector<u32> L = fetch(ere_losers.p, nl);
-            std::vector<u64> K = fetch(ere_key.p, nrec);
-            std::vector<u64> keys(nl);
-            for (u32 i = 0; i < nl; i++) keys[i] = K[L[i]];
-            std::sort(keys.begin(), keys.end());
-            big64b.reserve(rt, nl + 1);
-            rt.h2d(big64b.p, keys.data(), nl * 8);
+            // the losers' keys in ascending order, sorted on the device: by the low
+            // word (pair), then stably by the high word (elected rank)
+            big32a.reserve(rt, (size_t)nl + 1);
+            big32b.reserve(rt, (size_t)nl + 1);
+            work.reserve(rt, 2 * (size_t)nl + 2);
+            big64b.reserve(rt, (size_t)nl + 1);
+            radix_hist.reserve(rt, radix_hist_elems(nl));
+            radix_hscan.reserve(rt, radix_hist_elems(nl));
+            scan_tmp32.reserve(rt, scan_tmp_elems(radix_hist_elems(nl)) + 4);
+            rt.each(FEreLoserKey{ere_key.p, ere_losers.p, big32b.p, big32a.p, false}, nl);
+            radix_sort_pairs(big32a.p, big32b.p, work.p, work.p + nl + 1, nl, 32, radix_hist.p, radix_hscan.p,
+                             scan_tmp32.p, rt.stream);
+            rt.each(FEreLoserKey{ere_key.p, ere_losers.p, big32b.p, big32a.p, true}, nl);
+            const int rb = key_bits(npvs);
+            radix_sort_pairs(big32a.p, big32b.p, work.p, work.p + nl + 1, nl, rb, radix_hist.p, radix_hscan.p,
+                             scan_tmp32.p, rt.stream);
+            rt.launches += 5 * (4 + rb / 8);
+            rt.each(FEreLoserGather{ere_key.p, ere_losers.p, big32b.p, big64b.p}, nl);
             rt.one(FEreFix{a, big64b.p, nl});
-            rt.sync();
         }
     }
 

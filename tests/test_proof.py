@@ -9,7 +9,9 @@ src/cpu/proof.cpp).
   parser's) is in ours, and each extra line of ours either contains a literal of
   the round's final units (the reference leaves out an added clause that a unit
   assigned before it satisfies) or follows the point where an UNSAT round stops.
-* GPU: the CUDA build's proof holds the same lines as the emulation build's.
+* GPU: the CUDA build's proof holds the same lines as the emulation build's (for
+  a round that ends UNSAT, only the refutation is checked: the lines that the
+  other variables of the contradicting stage add depend on timing).
 """
 from collections import Counter
 
@@ -69,5 +71,6 @@ def test_proof_gpu(cuda_lib, built, name):
     status, pr, _ = _proof(cuda_lib, nv, lits, off)
     bad, refutes = orr.check_drat(nv, lits, off, pr)
     assert bad == -1 and refutes == (status == 1)
-    _, pe, _ = _proof(built["emu"], nv, lits, off)
-    assert Counter(orr.drat_lines(pr)) == Counter(orr.drat_lines(pe))
+    if status == 0:  # after a contradiction, what the stage's other variables add is timing
+        _, pe, _ = _proof(built["emu"], nv, lits, off)
+        assert Counter(orr.drat_lines(pr)) == Counter(orr.drat_lines(pe))
