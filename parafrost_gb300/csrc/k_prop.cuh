@@ -192,6 +192,73 @@ DEV void prop_lists_warp(const PropArgs& a, u32 k) {
 #endif
 HD void k_prop_clause(const PropArgs& a, u32 k) { prop_clause<false>(a, k); }
 
+// Sweep wave: when the pending literals' lists cover a large part of the store (a
+// propagation cascade), every clause of the store is checked against the current
+// assignment instead, in store order (streaming reads, no list walk, no collection):
+// a clause with a true literal is deleted, one with false literals loses them (a
+// unit is claimed, an empty clause is a conflict); a clause without an assigned
+// literal is left alone. Literals assigned during the sweep are pending for the next
+// wave, so the fixpoint is the one the list waves reach.
+template <bool Fresh>
+HD void prop_sweep_clause(const PropArgs& a, u32 r) {
+    const Ctx& c = a.c;
+    Hdr h = ldw_hdr<Fresh>(&c.hdr[r]);
+    if (h_deleted(h.flags)) return;
+    u32* l = c.lits + h.start;
+    u32 nfalse = 0;
+    for (u32 i = 0; i < h.size; i++) {
+        const int v = lit_value(c, ldw<Fresh>(&l[i]));
+        if (v == 1) {
+            c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+            touch(c, r);
+            return;
+        }
+        nfalse += v == 0;
+    }
+    if (!nfalse) return;
+    const u32 v0 = ABS(ldw<Fresh>(&l[0]));
+    u32 n = 0, sig = 0;
+    for (u32 i = 0; i < h.size; i++) {
+        const u32 lit = ldw<Fresh>(&l[i]);
+        if (lit_value(c, lit) == 0) continue;
+        l[n++] = lit;
+        sig |= MAPHASH(lit);
+    }
+    h.size = n;
+    h.sig = sig;
+    c.hdr[r] = h;
+    touch(c, r);
+    if (n == 0) {
+        set_unsat(c, v0);
+        if (c.var_fid) {
+            c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+            touch(c, r);
+        }
+        return;
+    }
+    if (n == 1) {
+        const u32 u = l[0];
+        const u32 old = atom_cas(&c.asg[ABS(u)], 0u, u);
+        if (old == 0) {
+            const u32 pos = atom_add(c.ntrail, 1u);
+            c.trail[pos] = u;
+            proof_line(c, &u, 1);
+        } else if (old != u) {
+            set_unsat(c, ABS(u));
+        }
+    }
+}
+HD void k_prop_sweep(const PropArgs& a, u32 r) { prop_sweep_clause<false>(a, r); }
+// The lists of a swept wave's literals end empty, as the list waves leave them.
+HD void k_prop_sweep_lists(const PropArgs& a, u32 k) {
+    const u32 t = a.c.trail[a.head + k];
+    a.c.ot_size[t] = 0;
+    a.c.ot_size[FLIP(t)] = 0;
+}
+// Sweep rather than walk: the pending literals' lists (estimated from the mean
+// list length) exceed a sixteenth of the store.
+HD bool prop_use_sweep(u32 pending, u32 occ_x16, u32 ncls) { return (u64)pending * occ_x16 > (u64)ncls; }
+
 #if SIGMA_CUDA
 // Every wave of one propagation in one cooperative launch: wave A over the trail
 // literals [head, tail), a grid barrier, wave B over the collected clauses, a
@@ -202,6 +269,7 @@ struct PropWaves {
     u32* bar;        // grid barrier words
     u32* waves;      // out: waves run
     u32 max_waves;
+    u32 occ_x16;     // 16 x mean occurrences per literal (sweep choice)
 };
 
 __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
@@ -222,6 +290,13 @@ __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
         b.stamp = a.stamp + wave;
         b.nwork = &w.nwork2[wave & 1];
         if (tid == 0) w.nwork2[(wave + 1) & 1] = 0;
+        if (prop_use_sweep(tail - head, w.occ_x16, a.c.ncls)) {
+            for (u32 r = tid; r < a.c.ncls; r += nth) prop_sweep_clause<true>(b, r);
+            for (u32 i = tid; i < tail - head; i += nth) k_prop_sweep_lists(b, i);
+            if (!grid_barrier(w.bar, a.c.err)) return;
+            head = tail;
+            continue;
+        }
         const u32 nwarps = nth >> 5;
         for (u32 i = tid >> 5; i < tail - head; i += nwarps) prop_lists_warp(b, i);
         if (!grid_barrier(w.bar, a.c.err)) return;

@@ -44,6 +44,8 @@ struct FGcFlags { Ctx c; u32* keep; u64* sizes; HD void operator()(u32 i) const 
 struct FGcMove { GcArgs a; HD void operator()(u32 i) const { k_gc_move(a, i); } };
 struct FPropLists { PropArgs a; HD void operator()(u32 i) const { k_prop_lists(a, i); } };
 struct FPropClause { PropArgs a; HD void operator()(u32 i) const { k_prop_clause(a, i); } };
+struct FPropSweep { PropArgs a; HD void operator()(u32 i) const { k_prop_sweep(a, i); } };
+struct FPropSweepLists { PropArgs a; HD void operator()(u32 i) const { k_prop_sweep_lists(a, i); } };
 struct FReduce { Ctx c; HD void operator()(u32 i) const { k_reduce_list(c, i); } };
 struct FScores { LcveArgs a; u32* max_score; HD void operator()(u32 i) const { k_scores(a, max_score, i); } };
 struct FRank { LcveArgs a; HD void operator()(u32 i) const { k_rank(a, i); } };
@@ -751,6 +753,9 @@ struct pf_sigma_ctx {
         alg_bytes += 2ull * (4ull * nlits_used + 8ull * ncls) + 8ull * D + 4ull * total;
     }
 
+    // 16 x the mean occurrence-list length (literals in use per literal slot).
+    u32 occ_x16() const { return (u32)std::min<u64>(16ull * nlits_used / std::max<u32>(D, 1), 0xFFFFFFFFull); }
+
     // prop (elimination.cpp:64-99).
     void prop() {
         if (prop_head >= ntrail) return;
@@ -770,7 +775,7 @@ struct pf_sigma_ctx {
             a.work = work.p;
             a.nwork = nullptr;
             a.cap_work = (u32)work.n;
-            PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, loop_bound()};
+            PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, loop_bound(), occ_x16()};
             rt.zero(counters.p + 22, 5 * 4);  // [22..23] work counters, [24..25] barrier, [26] waves
             void* args[] = {&a, &w};
             rt.launches++;
@@ -800,6 +805,14 @@ struct pf_sigma_ctx {
             a.work = work.p;
             a.nwork = counters.p + 2;
             a.cap_work = (u32)work.n;
+            if (prop_use_sweep(pend, occ_x16(), ncls)) {
+                rt.each(FPropSweep{a}, ncls);
+                rt.each(FPropSweepLists{a}, pend);
+                prop_head = ntrail;
+                ntrail = read_u32(counters.p + 0);
+                check();
+                continue;
+            }
             write_u32(counters.p + 2, 0);
             rt.each(FPropLists{a}, pend);
             const u32 nw = read_u32(counters.p + 2);
