@@ -65,7 +65,10 @@ typedef struct {
                               * A small value exercises the give-up path without any wait. */
     int32_t proof;           /* "proof" = 0: 1 records the round's DRAT proof (pf_sigma_proof);
                               * single formulas only */
-    int32_t reserved[5];
+    int32_t ot_buckets;      /* occurrence-table build: 0 by size (literal buckets once the
+                              * per-literal counters outgrow the L2 cache), 1 always literal
+                              * buckets, -1 always per-occurrence atomics */
+    int32_t reserved[4];
 } pf_options;
 
 /* Per-round statistics (the reference's stage report, src/cpu/statistics.cpp:28-41,

@@ -8,17 +8,17 @@
 //     one to its bucket in a per-block shared histogram; one atomic per bucket per
 //     block at the end. An exclusive scan of the bucket counts gives every bucket
 //     its range of the table (all its literals' lists, side by side).
-//   pass 1 (ot_bucket_fill_k): per tile of clauses, the same histogram in shared
-//     memory, one reservation per non-empty bucket, then each occurrence (literal,
-//     clause id) goes to its bucket's reserved run (two plain arrays).
+//   pass 1 (ot_bucket_fill_k): per tile of clauses, every occurrence (literal,
+//     clause id, one 8-byte word) is staged in shared memory and counted per
+//     bucket; a block scan orders the tile by bucket, one reservation per non-empty
+//     bucket gives each run its place, and the runs are written out contiguously
+//     (consecutive threads on consecutive words).
 //   pass 2 (ot_bucket_lists_k): one block per bucket: per-slot counts in shared
 //     memory, a block scan gives the list sizes and starts of the bucket's slots,
 //     then every occurrence lands in its list inside the bucket's range.
 // Clause headers and literals are read by whole warps, consecutive lanes on
-// consecutive literals. Equal keys inside a warp are combined (__match_any_sync)
-// before their shared-memory atomic, so a literal with millions of occurrences
-// costs one atomic per warp step. The order inside one list is unspecified, as for
-// the atomic build: the elected lists are sorted into the reference's order later.
+// consecutive literals. The order inside one list is unspecified, as for the
+// atomic build: the elected lists are sorted into the reference's order later.
 #pragma once
 
 #include "cnf.cuh"
@@ -27,7 +27,9 @@ namespace sigma {
 
 #if SIGMA_CUDA
 
-constexpr u32 OTB_TILE = 4096;      // clauses per block tile in passes 0 and 1
+constexpr u32 OTB_TILE = 4096;      // clauses per block tile in pass 0
+constexpr u32 OTB_FILL_TILE = 1024;  // clauses per block tile in pass 1 (staged in shared memory)
+constexpr u32 OTB_FILL_CAP = 8192;   // staged occurrences per pass-1 step
 constexpr u32 OTB_MAX_BUCKETS = 4096;
 constexpr u32 OTB_MAX_SHIFT = 15;   // 32,768 slots: 128 KiB of shared counters in pass 2
 constexpr u32 OTB_LIST_THREADS = 512;
@@ -40,8 +42,7 @@ struct OtbArgs {
     u32* count;       // nb: occurrences per bucket (pass 0)
     u32* cursor;      // nb: next free position of every bucket (pass 1; starts at base)
     const u32* base;  // nb + 1: first position of every bucket, base[nb] = occurrences
-    u32* tlit;        // occurrences grouped by bucket: literal
-    u32* tcid;        //   and clause id
+    u64* tpair;       // occurrences grouped by bucket: clause id << 32 | literal
 };
 
 // The literals of the live clauses id0 .. id0+n-1 (n <= 32), walked by one warp with
@@ -83,19 +84,6 @@ DEV void warp_clause_literals(const Ctx& c, u32 id0, u32 n, F&& f) {
     }
 }
 
-// Adds 1 for key to counter ctr[key] in shared memory from every valid lane; lanes
-// with the same key add together. Returns, for each valid lane, its rank among the
-// lanes of its key plus the counter's value before the add.
-DEV u32 warp_smem_rank(u32* ctr, bool valid, u32 key) {
-    const u32 lane = threadIdx.x & 31u;
-    const u32 peers = __match_any_sync(OTB_FULL, valid ? key : 0xffffffffu);
-    const u32 leader = __ffs(peers) - 1;
-    u32 old = 0;
-    if (valid && lane == leader) old = atomicAdd(&ctr[key], (u32)__popc(peers));
-    old = __shfl_sync(OTB_FULL, old, leader);
-    return old + (u32)__popc(peers & ((1u << lane) - 1u));
-}
-
 // Pass 0: occurrences per bucket.
 __global__ void __launch_bounds__(256) ot_bucket_count_k(OtbArgs a) {
     extern __shared__ u32 otb_hist[];
@@ -107,7 +95,7 @@ __global__ void __launch_bounds__(256) ot_bucket_count_k(OtbArgs a) {
         const u32 id0 = g * 32u;
         const u32 n = a.c.ncls - id0 < 32u ? a.c.ncls - id0 : 32u;
         warp_clause_literals(a.c, id0, n, [&](bool valid, u32 lit, u32) {
-            warp_smem_rank(otb_hist, valid, lit >> a.shift);
+            if (valid) atomicAdd(&otb_hist[lit >> a.shift], 1u);
         });
     }
     __syncthreads();
@@ -115,38 +103,98 @@ __global__ void __launch_bounds__(256) ot_bucket_count_k(OtbArgs a) {
         if (otb_hist[b]) atomicAdd(&a.count[b], otb_hist[b]);
 }
 
-// Pass 1: occurrences grouped by bucket, one reservation per bucket per tile.
-__global__ void __launch_bounds__(256) ot_bucket_fill_k(OtbArgs a) {
-    extern __shared__ u32 otb_sm[];
-    u32* hist = otb_sm;        // nb: tile counts, then ranks inside the tile
-    u32* run = otb_sm + a.nb;  // nb: the tile's reserved start in every bucket
-    const u32 warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const u32 ntiles = (a.c.ncls + OTB_TILE - 1u) / OTB_TILE;
-    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) hist[b] = 0;
-        __syncthreads();
-        const u32 c0 = t * OTB_TILE, c1 = a.c.ncls - c0 < OTB_TILE ? a.c.ncls : c0 + OTB_TILE;
-        for (u32 g = c0 + warp * 32u; g < c1; g += nw * 32u)
-            warp_clause_literals(a.c, g, c1 - g < 32u ? c1 - g : 32u, [&](bool valid, u32 lit, u32) {
-                warp_smem_rank(hist, valid, lit >> a.shift);
-            });
-        __syncthreads();
-        for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) {
-            const u32 n = hist[b];
-            run[b] = n ? atomicAdd(&a.cursor[b], n) : 0u;
-            hist[b] = 0;
+// Block-wide exclusive scan of cnt[0, n) in place; returns the total. Every thread
+// of the block calls it.
+DEV u32 otb_block_scan(u32* cnt, u32 n, u32* warp_tot, u32* carry) {
+    const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) *carry = 0;
+    __syncthreads();
+    for (u32 i0 = 0; i0 < n; i0 += blockDim.x) {
+        const u32 i = i0 + tid;
+        const u32 v = i < n ? cnt[i] : 0u;
+        u32 incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 t = __shfl_up_sync(OTB_FULL, incl, o);
+            if ((int)lane >= o) incl += t;
         }
+        if (lane == 31) warp_tot[warp] = incl;
+        __syncthreads();
+        u32 before = *carry;
+        for (u32 w = 0; w < warp; w++) before += warp_tot[w];
+        if (i < n) cnt[i] = before + incl - v;
+        __syncthreads();
+        if (tid == blockDim.x - 1) *carry = before + incl;
+        __syncthreads();
+    }
+    return *carry;
+}
+
+// Pass 1: occurrences grouped by bucket. A tile's occurrences are counted per
+// bucket and staged in shared memory in arrival order; one reservation per
+// non-empty bucket gives each run its place; the staged occurrences are ordered by
+// bucket (a block scan of the counts) and each run is written contiguously. A tile
+// with more occurrences than the stage holds (very long clauses) writes them to
+// their runs directly instead.
+constexpr u32 OTB_FILL_THREADS = 512;
+__global__ void __launch_bounds__(OTB_FILL_THREADS) ot_bucket_fill_k(OtbArgs a) {
+    extern __shared__ u64 otb_fsm[];
+    u64* stage = otb_fsm;                                           // OTB_FILL_CAP
+    u64* sorted = otb_fsm + OTB_FILL_CAP;                           // OTB_FILL_CAP
+    u32* cnt = reinterpret_cast<u32*>(otb_fsm + 2 * OTB_FILL_CAP);  // nb: counts, then tile offsets
+    u32* run = cnt + a.nb;                                          // nb: global start of the tile's run
+    u32* cur = run + a.nb;                                          // nb: cursors
+    __shared__ u32 warp_tot[OTB_FILL_THREADS / 32];
+    __shared__ u32 carry, nstage;
+    const u32 lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const u32 ntiles = (a.c.ncls + OTB_FILL_TILE - 1u) / OTB_FILL_TILE;
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const u32 c0 = t * OTB_FILL_TILE, c1 = a.c.ncls - c0 < OTB_FILL_TILE ? a.c.ncls : c0 + OTB_FILL_TILE;
+        for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) cnt[b] = 0;
+        if (threadIdx.x == 0) nstage = 0;
         __syncthreads();
         for (u32 g = c0 + warp * 32u; g < c1; g += nw * 32u)
             warp_clause_literals(a.c, g, c1 - g < 32u ? c1 - g : 32u, [&](bool valid, u32 lit, u32 cid) {
-                const u32 b = lit >> a.shift;
-                const u32 r = warp_smem_rank(hist, valid, b);
+                const unsigned m = __ballot_sync(OTB_FULL, valid);
+                u32 base = 0;
+                if (lane == 0 && m) base = atomicAdd(&nstage, (u32)__popc(m));
+                base = __shfl_sync(OTB_FULL, base, 0);
                 if (valid) {
-                    const u32 pos = run[b] + r;
-                    a.tlit[pos] = lit;
-                    a.tcid[pos] = cid;
+                    const u32 pos = base + (u32)__popc(m & ((1u << lane) - 1u));
+                    if (pos < OTB_FILL_CAP) stage[pos] = ((u64)cid << 32) | lit;
+                    atomicAdd(&cnt[lit >> a.shift], 1u);
                 }
             });
+        __syncthreads();
+        const u32 n = nstage;
+        for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) {
+            const u32 k = cnt[b];
+            run[b] = k ? atomicAdd(&a.cursor[b], k) : 0u;
+        }
+        if (n <= OTB_FILL_CAP) {
+            otb_block_scan(cnt, a.nb, warp_tot, &carry);
+            for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) cur[b] = cnt[b];
+            __syncthreads();
+            for (u32 i = threadIdx.x; i < n; i += blockDim.x) {
+                const u64 x = stage[i];
+                sorted[atomicAdd(&cur[(u32)x >> a.shift], 1u)] = x;
+            }
+            __syncthreads();
+            for (u32 i = threadIdx.x; i < n; i += blockDim.x) {
+                const u64 x = sorted[i];
+                const u32 b = (u32)x >> a.shift;
+                a.tpair[run[b] + (i - cnt[b])] = x;
+            }
+        } else {
+            for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) cur[b] = 0;
+            __syncthreads();
+            for (u32 g = c0 + warp * 32u; g < c1; g += nw * 32u)
+                warp_clause_literals(a.c, g, c1 - g < 32u ? c1 - g : 32u, [&](bool valid, u32 lit, u32 cid) {
+                    if (!valid) return;
+                    const u32 b = lit >> a.shift;
+                    a.tpair[run[b] + atomicAdd(&cur[b], 1u)] = ((u64)cid << 32) | lit;
+                });
+        }
         __syncthreads();
     }
 }
@@ -165,12 +213,7 @@ __global__ void __launch_bounds__(OTB_LIST_THREADS) ot_bucket_lists_k(OtbArgs a)
     for (u32 i = tid; i < nl; i += blockDim.x) otb_cnt[i] = 0;
     if (tid == 0) carry = 0;
     __syncthreads();
-    for (u32 k0 = p0; k0 < p1; k0 += blockDim.x) {
-        const u32 k = k0 + tid;
-        const bool valid = k < p1;
-        const u32 lit = valid ? __ldcs(&a.tlit[k]) : l0;
-        warp_smem_rank(otb_cnt, valid, lit - l0);
-    }
+    for (u32 k = p0 + tid; k < p1; k += blockDim.x) atomicAdd(&otb_cnt[(u32)__ldcg(&a.tpair[k]) - l0], 1u);
     __syncthreads();
     // block scan of the slot counts, blockDim.x slots per step: list sizes and starts
     for (u32 i0 = 0; i0 < nl; i0 += blockDim.x) {
@@ -196,13 +239,9 @@ __global__ void __launch_bounds__(OTB_LIST_THREADS) ot_bucket_lists_k(OtbArgs a)
         if (tid == blockDim.x - 1) carry = excl + v;
         __syncthreads();
     }
-    for (u32 k0 = p0; k0 < p1; k0 += blockDim.x) {
-        const u32 k = k0 + tid;
-        const bool valid = k < p1;
-        const u32 lit = valid ? __ldcs(&a.tlit[k]) : l0;
-        const u32 cid = valid ? __ldcs(&a.tcid[k]) : 0u;
-        const u32 pos = warp_smem_rank(otb_cnt, valid, lit - l0);
-        if (valid) a.c.ot_refs[p0 + pos] = cid;
+    for (u32 k = p0 + tid; k < p1; k += blockDim.x) {
+        const u64 x = __ldcs(&a.tpair[k]);
+        a.c.ot_refs[p0 + atomicAdd(&otb_cnt[(u32)x - l0], 1u)] = (u32)(x >> 32);
     }
 }
 

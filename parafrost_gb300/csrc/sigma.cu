@@ -674,9 +674,14 @@ struct pf_sigma_ctx {
     // ------------------------------------------------------------ stages
 #if SIGMA_CUDA
     // Occurrence table by literal buckets (k_otb.cuh): buckets of 2^shift literal
-    // slots, at most OTB_MAX_BUCKETS of them (so up to 134M literal slots).
-    DBuf<u32> otb_count, otb_base, otb_cursor, otb_lit, otb_cid;
+    // slots, at most OTB_MAX_BUCKETS of them (so up to 134M literal slots). Used when
+    // the per-literal counters (4 bytes a slot) outgrow the L2 cache, where the
+    // atomic histogram and scatter turn into random device-memory traffic.
+    static constexpr u64 kOtbMinSlots = 1ull << 24;
+    DBuf<u32> otb_count, otb_base, otb_cursor;
+    DBuf<u64> otb_pair;
     bool otb_plan(u32& shift, u32& nb) const {
+        if (opt.ot_buckets < 0 || (opt.ot_buckets == 0 && D < kOtbMinSlots)) return false;
         u32 s = 8;
         while (s < OTB_MAX_SHIFT && ((u64)D >> s) > 1024) s++;
         shift = s;
@@ -687,14 +692,17 @@ struct pf_sigma_ctx {
         otb_count.reserve(rt, nb + 1);
         otb_base.reserve(rt, nb + 1);
         otb_cursor.reserve(rt, nb + 1);
-        otb_lit.reserve(rt, (size_t)nlits_used + 1);
-        otb_cid.reserve(rt, (size_t)nlits_used + 1);
+        otb_pair.reserve(rt, (size_t)nlits_used + 1);
         rt.zero(otb_count.p, (size_t)nb * 4);
-        OtbArgs a{view(), shift, nb, otb_count.p, otb_cursor.p, otb_base.p, otb_lit.p, otb_cid.p};
+        OtbArgs a{view(), shift, nb, otb_count.p, otb_cursor.p, otb_base.p, otb_pair.p};
+        const u32 fill_smem = 2 * OTB_FILL_CAP * 8 + 3 * nb * 4;
         static bool attr_set = false;
         if (!attr_set) {
             ck(cudaFuncSetAttribute(ot_bucket_lists_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)((1u << OTB_MAX_SHIFT) * 4)),
+               "smem attr");
+            ck(cudaFuncSetAttribute(ot_bucket_fill_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(2 * OTB_FILL_CAP * 8 + 3 * OTB_MAX_BUCKETS * 4)),
                "smem attr");
             attr_set = true;
         }
@@ -706,10 +714,10 @@ struct pf_sigma_ctx {
         }
         scan1_launch(otb_count.p, otb_base.p, nb, otb_base.p + nb);
         rt.d2d(otb_cursor.p, otb_base.p, (size_t)nb * 4);
-        const u32 ntiles = (ncls + OTB_TILE - 1) / OTB_TILE;
+        const u32 ntiles = (ncls + OTB_FILL_TILE - 1) / OTB_FILL_TILE;
         if (ntiles) {
             rt.launches++;
-            ot_bucket_fill_k<<<std::min(grid, ntiles), 256, 2 * nb * 4, rt.stream>>>(a);
+            ot_bucket_fill_k<<<std::min((u32)rt.sms * 2u, ntiles), OTB_FILL_THREADS, fill_smem, rt.stream>>>(a);
             ck(cudaGetLastError(), "launch");
         }
         rt.launches++;
@@ -2650,8 +2658,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     c.otb_count.free();
     c.otb_base.free();
     c.otb_cursor.free();
-    c.otb_lit.free();
-    c.otb_cid.free();
+    c.otb_pair.free();
 #endif
     c.pv_perm.free();
     c.pv_key.free();

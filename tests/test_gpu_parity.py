@@ -86,3 +86,27 @@ def test_gpu_sub_rerun(cuda_lib, built, case, opt):
     stats, b, _ = run_lib(cuda_lib, nv, lits, off, opts, level=2)
     assert stats.status == st
     assert rd.compare(rd.normalize(a), rd.normalize(b)) == []
+
+
+@pytest.mark.parametrize("case", [c[0] for c in CASES])
+def test_gpu_stagewise_bucketed_ot(cuda_lib, built, case):
+    """The literal-bucket occurrence-table build (chosen by size for large formulas)
+    forced on every formula, stage by stage against the oracle."""
+    nv, lits, off = dict(CASES)[case](23)
+    st, a, _ = orr.run_oracle(nv, lits, off, Options(all=1), level=2)
+    stats, b, _ = run_lib(cuda_lib, nv, lits, off, Options(all=1, ot_buckets=1), level=2)
+    assert stats.status == st
+    assert rd.compare(rd.normalize(a), rd.normalize(b)) == []
+
+
+@pytest.mark.parametrize("gen", [
+    lambda: cnfgen.community(num_vars=200_000, num_clauses=800_000, seed=6),
+    lambda: cnfgen.aig_tseitin(num_inputs=5000, num_and=200_000, num_xor=20_000, seed=5),
+])
+def test_gpu_canonical_bucketed_ot(cuda_lib, built, gen):
+    nv, lits, off = gen()
+    st, a, _ = orr.run_oracle(nv, lits, off, Options(all=1), level=1)
+    stats, b, _ = run_lib(cuda_lib, nv, lits, off, Options(all=1, ot_buckets=1), level=1)
+    assert stats.status == st
+    assert rd.canonical(a) == rd.canonical(b)
+    assert rd.compare(a, b, kinds=("pvs", "counts", "elim")) == []
