@@ -134,6 +134,7 @@ def cpu_round_seconds(nv, lits, off) -> tuple:
 
 
 FORMULAS = None  # --formulas: a smaller batch of the same generator (quick runs)
+EXTRA_OPTS: dict = {}  # --opt NAME=VALUE for the single-formula workloads
 
 
 def batch_forms(name: str):
@@ -288,7 +289,7 @@ def run_ours(args) -> dict:
     d_lits = torch.from_numpy(lits.view(np.int32)).to(dev)
     d_off = torch.from_numpy(off.view(np.int64)).to(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    opts = Options(all=1)
+    opts = Options(all=1, **EXTRA_OPTS)
     s = Simplifier(opts)
 
     def step():
@@ -389,8 +390,8 @@ def run_ours(args) -> dict:
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
            "config": {"workload": args.workload, "clauses": int(ncls), "literals": int(lits.size), "vars": int(nv),
-                      "options": "-all, phases=5", "l2": "flushed between steps (256 MB write)",
-                      "parallelism": f"replicas x{world}"},
+                      "options": "-all, phases=5" + "".join(f", {k}={v}" for k, v in EXTRA_OPTS.items()),
+                      "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
            "round_ms": round_ms, "stage_ms": stage_ms,
            "result": {"clauses_after": int(last.clauses_after), "phases": int(last.phases_run),
                       "status": int(last.status), "mis_rounds": int(last.mis_rounds),
@@ -634,7 +635,11 @@ def main():
     ap.add_argument("--no-sequential", action="store_true", help="batched workload: skip the one-by-one comparison")
     ap.add_argument("--formulas", type=int, default=None, help="batched workload: number of formulas")
     ap.add_argument("--requests", type=int, default=160, help="serving workload: requests per arrival rate")
+    ap.add_argument("--opt", action="append", default=[], metavar="NAME=VALUE",
+                    help="a simplifier option for the single-formula workloads (e.g. ot_buckets=1)")
     args = ap.parse_args()
+    global EXTRA_OPTS
+    EXTRA_OPTS = {k: int(v) for k, v in (o.split("=", 1) for o in args.opt)}
     global FORMULAS
     FORMULAS = args.formulas
     if args.impl == "reference":
