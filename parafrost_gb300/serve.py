@@ -1,17 +1,20 @@
 """Serving loop: simplification requests arrive over time and are answered by
 batched sigmify rounds on one GPU.
 
-A request is one formula. A worker thread takes every request that is waiting
-when it becomes free, admits them in arrival order while their estimated device
-footprint fits its share of the HBM budget (and the batch's formula cap), and
-runs one batched round over them (``pf_sigma_upload_batch`` -> ``pf_sigma_round``
--> ``pf_sigma_batch_download``): each formula gets exactly the result of its own
-round. Batched mode runs two workers, each with its own context and stream, so one
-batch's copies and host work overlap the other's kernels on the device, and
-requests that arrive while a batch runs are admitted as soon as a worker is free.
-In ``plain`` mode one worker runs every request alone through the single-formula
-calls instead, the comparison point for batching. Latency is measured from a
-request's arrival to the moment its result is on the host.
+A request is one formula. Requests go to a lane by size (small and large). A
+worker thread of a lane takes every request waiting in the lane when it becomes
+free, admits them in arrival order while their estimated device footprint fits
+its share of the HBM budget (and the batch's formula cap), and runs one batched
+round over them (``pf_sigma_upload_batch`` -> ``pf_sigma_round`` ->
+``pf_sigma_batch_download``): each formula gets exactly the result of its own
+round. Batched mode runs two workers per lane, each with its own context and
+stream: the batches of all workers are on the device at once, one batch's copies
+and host work overlap the others' kernels, a request that arrives while batches
+run is admitted by the next worker of its lane that frees up, and a small request
+never waits behind a large one. In ``plain`` mode one worker runs every request
+alone through the single-formula calls instead, the comparison point for
+batching. Latency is measured from a request's arrival to the moment its result
+is on the host.
 
 There is no counterpart in the reference (ParaFROST simplifies the formula of one
 solver object inside ``sigmify()``); the per-formula work is the reference's
@@ -60,11 +63,20 @@ class Request:
 
 
 class Server:
-    """One GPU; worker threads (two in batched mode, one in plain mode), each with
-    its own context; requests admitted in arrival order."""
+    """One GPU; worker threads, each with its own context and stream, in lanes by
+    request size; requests admitted in arrival order within a lane.
+
+    Batched mode has two lanes: requests of up to ``small_clauses`` clauses go to
+    the small lane, larger ones to the large lane, each lane with its own queue and
+    workers, so a small request never waits behind a multi-million-clause batch. A
+    lane's free worker admits every request waiting in its lane (while it fits the
+    worker's share of the HBM budget) into its next batched round; the workers'
+    rounds overlap on the device. Plain mode has one lane and one worker that runs
+    each request alone."""
 
     def __init__(self, opts: Options | None = None, hbm_budget: int = 64 << 30, max_batch: int = 4096,
-                 mode: str = "batched", library: str | None = None, workers: int | None = None):
+                 mode: str = "batched", library: str | None = None, workers: int | None = None,
+                 small_clauses: int = 200_000, lanes: int | None = None):
         if mode not in ("batched", "plain"):
             raise ValueError("mode is 'batched' or 'plain'")
         self.opts = opts or Options(all=1)
@@ -72,16 +84,26 @@ class Server:
         self.max_batch = int(max_batch)
         self.mode = mode
         self.library = library
-        self.workers = int(workers) if workers else (2 if mode == "batched" else 1)
+        self.lanes = int(lanes) if lanes else (2 if mode == "batched" else 1)
+        self.small_clauses = int(small_clauses)
+        # workers per lane
+        self.per_lane = int(workers) if workers else (2 if mode == "batched" else 1)
+        self.workers = self.per_lane * self.lanes
         self.worker_budget = self.hbm_budget // self.workers
-        self.q: queue.Queue = queue.Queue()
+        self.queues: list = [queue.Queue() for _ in range(self.lanes)]
+        self.q = self.queues[0]
         self.batches: list = []          # (formulas, clauses, estimated bytes, device bytes held after, launches)
         self.max_footprint = 0           # device bytes held by all workers' contexts at once, at most
         self._held: list = [0] * self.workers
         self._lock = threading.Lock()
+        self._lane_locks = [threading.Lock() for _ in range(self.lanes)]
         self._stop = threading.Event()
         self._threads: list = []
-        self._pending: list = []
+        self._pending: list = [[] for _ in range(self.lanes)]
+
+    def lane_of(self, formula: tuple) -> int:
+        """The lane of a request: 0 (small) or the last (large) by clause count."""
+        return 0 if self.lanes == 1 or formula[2].size - 1 <= self.small_clauses else self.lanes - 1
 
     # ---- client side
     def submit(self, formula: tuple, arrival: float | None = None) -> Request:
@@ -90,7 +112,7 @@ class Server:
         if estimate_footprint(nv, off.size - 1, lits.size) > self.worker_budget:
             self._finish(r, -2, error="request larger than the HBM budget")
             return r
-        self.q.put(r)
+        self.queues[self.lane_of(formula)].put(r)
         return r
 
     def start(self) -> "Server":
@@ -117,22 +139,24 @@ class Server:
         r.finished = time.perf_counter()
         r.done.set()
 
-    def _admit(self) -> list:
-        """The next batch (called under the lock): waiting requests in arrival order
-        while they fit one worker's budget; [] once stopped with nothing waiting."""
-        reqs = self._pending
-        self._pending = []
+    def _admit(self, lane: int) -> list:
+        """The next batch of a lane (called under the lane's lock): waiting requests in
+        arrival order while they fit one worker's budget; [] once stopped with
+        nothing waiting."""
+        q = self.queues[lane]
+        reqs = self._pending[lane]
+        self._pending[lane] = []
         while not reqs:
-            if self._stop.is_set() and self.q.empty():
+            if self._stop.is_set() and q.empty():
                 return []
             try:
-                r = self.q.get(timeout=0.02)
+                r = q.get(timeout=0.02)
             except queue.Empty:
                 continue
             reqs = [r]
         while True:
             try:
-                reqs.append(self.q.get_nowait())
+                reqs.append(q.get_nowait())
             except queue.Empty:
                 break
         batch, used = [], 0
@@ -140,27 +164,29 @@ class Server:
             nv, lits, off = r.formula
             need = estimate_footprint(nv, off.size - 1, lits.size)
             if batch and (used + need > self.worker_budget or len(batch) >= self.max_batch):
-                self._pending = reqs[i:]
+                self._pending[lane] = reqs[i:]
                 break
             batch.append(r)
             used += need
         return batch
 
     def _run(self, w: int) -> None:
+        lane = w % self.lanes
         try:
             ctx = Simplifier(self.opts, library=self.library)
         except Exception as e:  # no context: this worker answers what it admits with the error
             while True:
-                with self._lock:
-                    batch = self._admit()
+                with self._lane_locks[lane]:
+                    batch = self._admit(lane)
                 if not batch:
                     return
                 for r in batch:
                     self._finish(r, getattr(e, "status", -4), error=str(e))
         try:
             while True:
+                with self._lane_locks[lane]:
+                    batch = self._admit(lane)
                 with self._lock:
-                    batch = self._admit()
                     bi = len(self.batches)
                     if batch:
                         self.batches.append(None)  # this batch's slot, filled below

@@ -46,7 +46,7 @@ def test_serve_admission(built):
     budget = max(need) * 2 + 1
     big = cnfgen.aig_unrolled(num_gates=400, steps=20, seed=9)
     assert estimate_footprint(big[0], big[2].size - 1, big[1].size) > budget
-    srv = Server(Options(all=1), hbm_budget=budget, library=built["emu"])
+    srv = Server(Options(all=1), hbm_budget=budget, library=built["emu"], lanes=1)
     reqs = [srv.submit(f) for f in reqs_f]  # queued before the server starts: one admission pass
     refused = srv.submit(big)
     srv.start()
@@ -94,3 +94,23 @@ def test_serve_without_library_fails_requests():
         for r in reqs:
             assert r.wait(30)
     assert all(r.status is not None and r.status < 0 and r.error for r in reqs)
+
+
+def test_serve_lanes(built):
+    """Small and large requests go to separate lanes; every result is still the
+    request's own round."""
+    opts = Options(all=1)
+    small = small_requests(6, seed=8)
+    large = [cnfgen.aig_unrolled(num_gates=300, steps=12, seed=12 + i) for i in range(2)]
+    sizes = sorted(f[2].size - 1 for f in small + large)
+    cut = (max(f[2].size - 1 for f in small) + min(f[2].size - 1 for f in large)) // 2
+    assert max(f[2].size - 1 for f in small) < cut < min(f[2].size - 1 for f in large), sizes
+    with Server(opts, library=built["emu"], small_clauses=cut) as srv:
+        assert srv.lanes == 2 and srv.workers == 4
+        assert {srv.lane_of(f) for f in small} == {0} and {srv.lane_of(f) for f in large} == {1}
+        reqs = [srv.submit(f) for f in large + small]
+        for r in reqs:
+            assert r.wait(120)
+    for f, r in zip(large + small, reqs):
+        want, ph = own_round(built["emu"], f, opts)
+        assert rd.canonical_result(r.status, r.result) == want
