@@ -248,6 +248,29 @@ pf_status pf_sigma_batch_result_sizes(pf_sigma_ctx* ctx, int32_t* status, uint32
 pf_status pf_sigma_batch_download(pf_sigma_ctx* ctx, uint32_t* lits, uint64_t* offsets, uint8_t* learnt,
                                   uint32_t* units, uint32_t* resolved, uint8_t* eliminated);
 
+/* A formula in host memory, as pf_dimacs_parse returns it: clause c has literals
+ * lits[offsets[c] .. offsets[c+1]) (2*var + sign); the arrays belong to the library
+ * and are released by pf_formula_free. */
+typedef struct {
+    uint32_t num_vars;
+    uint64_t num_clauses;
+    uint32_t* lits;
+    uint64_t* offsets;  /* num_clauses + 1 */
+    int32_t empty_clause; /* 1: the file holds an empty clause (the formula is unsatisfiable) */
+} pf_formula;
+
+/* Reads a DIMACS CNF file (ParaFROST::parser, src/cpu/dimacs.cpp:25-176): comments,
+ * the "p cnf V C" header, clauses ended by 0. As the reference's toClause() does, a
+ * repeated literal is dropped, a tautological clause is dropped and a variable above
+ * V is an error (PF_EINVAL, text in pf_last_error). Every other clause is kept as
+ * written, one-literal clauses included (pf_sigma_upload turns them into units); an
+ * empty clause sets empty_clause and returns PF_UNSAT (the reference drops a clause
+ * that its earlier units falsify; this reader keeps the contradiction). */
+pf_status pf_dimacs_parse(const char* path, pf_formula* out);
+
+/* Releases the arrays of a formula from pf_dimacs_parse. */
+void pf_formula_free(pf_formula* f);
+
 /* Device bytes held by the context. */
 pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes);
 

@@ -5,6 +5,7 @@
 #include "../../include/sigma_gb300.h"
 
 #include "cnf.cuh"
+#include "dimacs.h"
 #include "k_bce_ere.cuh"
 #include "k_bve.cuh"
 #include "k_lcve.cuh"
@@ -2613,6 +2614,37 @@ pf_status pf_create_ot_noalloc(uint32_t num_vars, const uint32_t* d_lits, const 
 }
 
 uint64_t pf_device_alloc_count(void) { return device_alloc_count().load(); }
+
+pf_status pf_dimacs_parse(const char* path, pf_formula* out) {
+    if (!path || !out) return fail("null argument", PF_EINVAL);
+    std::memset(out, 0, sizeof(*out));
+    return guarded([&]() -> pf_status {
+        DimacsFormula f;
+        const std::string err = dimacs_read(path, f);
+        if (!err.empty()) return fail(std::string("DIMACS: ") + err, PF_EINVAL);
+        const size_t nc = f.offsets.size() - 1;
+        out->num_vars = f.num_vars;
+        out->num_clauses = nc;
+        out->lits = (uint32_t*)std::malloc(std::max<size_t>(f.lits.size(), 1) * 4);
+        out->offsets = (uint64_t*)std::malloc((nc + 1) * 8);
+        if (!out->lits || !out->offsets) {
+            pf_formula_free(out);
+            return fail("out of host memory", PF_ENOMEM);
+        }
+        if (!f.lits.empty()) std::memcpy(out->lits, f.lits.data(), f.lits.size() * 4);
+        std::memcpy(out->offsets, f.offsets.data(), (nc + 1) * 8);
+        out->empty_clause = f.empty_clause ? 1 : 0;
+        return f.empty_clause ? PF_UNSAT : PF_OK;
+    });
+}
+
+void pf_formula_free(pf_formula* f) {
+    if (!f) return;
+    std::free(f->lits);
+    std::free(f->offsets);
+    f->lits = nullptr;
+    f->offsets = nullptr;
+}
 
 pf_status pf_sigma_footprint(pf_sigma_ctx* ctx, uint64_t* bytes) {
     if (!ctx || !bytes) return fail("null argument", PF_EINVAL);

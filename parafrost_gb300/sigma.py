@@ -110,6 +110,10 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     lib.pf_create_ot.restype = ctypes.c_int
     lib.pf_device_alloc_count.argtypes = []
     lib.pf_device_alloc_count.restype = ctypes.c_uint64
+    lib.pf_dimacs_parse.argtypes = [ctypes.c_char_p, _VP]
+    lib.pf_dimacs_parse.restype = ctypes.c_int
+    lib.pf_formula_free.argtypes = [_VP]
+    lib.pf_formula_free.restype = None
     lib.pf_last_error.argtypes = []
     lib.pf_last_error.restype = ctypes.c_char_p
     return lib
@@ -127,6 +131,30 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             raise SigmaError(PF_EDEVICE, f"CUDA library not built: {path} (run __graft_entry__.build())")
         _LIBS[path] = _bind(ctypes.CDLL(path))
     return _LIBS[path]
+
+
+class PfFormula(ctypes.Structure):
+    _fields_ = [("num_vars", ctypes.c_uint32), ("num_clauses", ctypes.c_uint64),
+                ("lits", ctypes.POINTER(ctypes.c_uint32)), ("offsets", ctypes.POINTER(ctypes.c_uint64)),
+                ("empty_clause", ctypes.c_int32)]
+
+
+def read_dimacs(path: str, library: str | None = None):
+    """(num_vars, lits, offsets, empty_clause) of a DIMACS file, read by the library's
+    reader (pf_dimacs_parse)."""
+    lib = load_library(library)
+    f = PfFormula()
+    st = lib.pf_dimacs_parse(path.encode(), ctypes.byref(f))
+    if st not in (PF_OK, PF_UNSAT):
+        raise SigmaError(st, lib.pf_last_error().decode(errors="replace"))
+    try:
+        n, nl = int(f.num_clauses), 0
+        off = np.ctypeslib.as_array(f.offsets, shape=(n + 1,)).copy()
+        nl = int(off[-1])
+        lits = np.ctypeslib.as_array(f.lits, shape=(max(nl, 1),))[:nl].copy()
+    finally:
+        lib.pf_formula_free(ctypes.byref(f))
+    return int(f.num_vars), lits.astype(np.uint32), off.astype(np.uint64), bool(f.empty_clause)
 
 
 def _ptr(a: np.ndarray | None):
