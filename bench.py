@@ -445,7 +445,14 @@ def run_ours_batch(args) -> dict:
     d_lits = torch.from_numpy(lits.view(np.int32)).to(dev)
     d_off = torch.from_numpy(off.view(np.int64)).to(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    s = Simplifier(Options(all=1))
+    opts = Options(all=1, **EXTRA_OPTS)
+    tuned = None
+    if args.tune:
+        # launch-shape knobs tuned on every 32nd formula of the batch (untimed)
+        from parafrost_gb300.tune import tune
+        opts, seen = tune(forms[::32], opts, repeats=3)
+        tuned = {"chosen": {k: getattr(opts, k) for k in seen}, "round_ms": seen, "sample": f"every 32nd of {nf} formulas"}
+    s = Simplifier(opts)
 
     def step():
         s.upload_batch_device(nv, cb, d_lits.data_ptr(), d_off.data_ptr())
@@ -532,7 +539,7 @@ def run_ours_batch(args) -> dict:
     if not args.no_sequential:
         step_k = max(1, nf // 128)
         sample = forms[::step_k][:128]
-        one = Simplifier(Options(all=1))
+        one = Simplifier(opts)
         dl = [(torch.from_numpy(np.asarray(l, dtype=np.uint32).view(np.int32)).to(dev),
                torch.from_numpy(np.asarray(o, dtype=np.uint64).view(np.int64)).to(dev), v) for v, l, o in sample]
         for dlits, doff, v in dl[:3]:  # warm-up
@@ -559,6 +566,7 @@ def run_ours_batch(args) -> dict:
            "result": {"clauses_after": int(last.clauses_after), "phases": int(last.phases_run),
                       "launches_per_round": int(last.kernel_launches)},
            "sequential_cnfs_per_s": seq,
+           "tuned": tuned,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": profiled_traffic(dom, args.workload), "kernel": dom,
                         "algorithmic_bytes_per_launch": kern[dom]["bytes_per_launch"],
@@ -635,6 +643,7 @@ def main():
     ap.add_argument("--no-sequential", action="store_true", help="batched workload: skip the one-by-one comparison")
     ap.add_argument("--formulas", type=int, default=None, help="batched workload: number of formulas")
     ap.add_argument("--requests", type=int, default=160, help="serving workload: requests per arrival rate")
+    ap.add_argument("--tune", action="store_true", help="batched workload: autotune the launch knobs first")
     ap.add_argument("--opt", action="append", default=[], metavar="NAME=VALUE",
                     help="a simplifier option for the single-formula workloads (e.g. ot_buckets=1)")
     args = ap.parse_args()

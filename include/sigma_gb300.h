@@ -68,7 +68,10 @@ typedef struct {
     int32_t ot_buckets;      /* occurrence-table build: 0 by size (literal buckets once the
                               * per-literal counters outgrow the L2 cache), 1 always literal
                               * buckets, -1 always per-occurrence atomics */
-    int32_t reserved[4];
+    int32_t sweep_div;       /* propagation sweeps the whole store when the pending literals'
+                              * lists exceed 1/sweep_div of it: 0 = 16, -1 never sweeps */
+    int32_t pv_blocks;       /* blocks per SM of the per-variable warp kernels: 0 = 8 */
+    int32_t reserved[2];
 } pf_options;
 
 /* Per-round statistics (the reference's stage report, src/cpu/statistics.cpp:28-41,

@@ -255,9 +255,10 @@ HD void k_prop_sweep_lists(const PropArgs& a, u32 k) {
     a.c.ot_size[t] = 0;
     a.c.ot_size[FLIP(t)] = 0;
 }
-// Sweep rather than walk: the pending literals' lists (estimated from the mean
-// list length) exceed a sixteenth of the store.
-HD bool prop_use_sweep(u32 pending, u32 occ_x16, u32 ncls) { return (u64)pending * occ_x16 > (u64)ncls; }
+// Sweep rather than walk: the pending literals' lists (estimated from the mean list
+// length) exceed a fraction of the store; scale = mean list length x the divisor of
+// that fraction (0: never sweep).
+HD bool prop_use_sweep(u32 pending, u32 scale, u32 ncls) { return scale && (u64)pending * scale > (u64)ncls; }
 
 #if SIGMA_CUDA
 // Every wave of one propagation in one cooperative launch: wave A over the trail
@@ -269,7 +270,7 @@ struct PropWaves {
     u32* bar;        // grid barrier words
     u32* waves;      // out: waves run
     u32 max_waves;
-    u32 occ_x16;     // 16 x mean occurrences per literal (sweep choice)
+    u32 sweep_scale; // mean occurrences per literal x sweep divisor (0: never sweep)
 };
 
 __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
         b.stamp = a.stamp + wave;
         b.nwork = &w.nwork2[wave & 1];
         if (tid == 0) w.nwork2[(wave + 1) & 1] = 0;
-        if (prop_use_sweep(tail - head, w.occ_x16, a.c.ncls)) {
+        if (prop_use_sweep(tail - head, w.sweep_scale, a.c.ncls)) {
             for (u32 r = tid; r < a.c.ncls; r += nth) prop_sweep_clause<true>(b, r);
             for (u32 i = tid; i < tail - head; i += nth) k_prop_sweep_lists(b, i);
             if (!grid_barrier(w.bar, a.c.err)) return;

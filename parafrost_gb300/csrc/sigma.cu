@@ -762,8 +762,15 @@ struct pf_sigma_ctx {
         alg_bytes += 2ull * (4ull * nlits_used + 8ull * ncls) + 8ull * D + 4ull * total;
     }
 
-    // 16 x the mean occurrence-list length (literals in use per literal slot).
-    u32 occ_x16() const { return (u32)std::min<u64>(16ull * nlits_used / std::max<u32>(D, 1), 0xFFFFFFFFull); }
+    // The mean occurrence-list length (literals in use per literal slot) times the
+    // sweep divisor, 0 when sweeps are off (prop_use_sweep).
+    u32 sweep_scale() const {
+        if (opt.sweep_div < 0) return 0;
+        const u64 div = opt.sweep_div ? (u64)opt.sweep_div : 16ull;
+        return (u32)std::min<u64>(std::max<u64>(div * nlits_used / std::max<u32>(D, 1), 1), 0xFFFFFFFFull);
+    }
+    // Blocks of the per-variable warp kernels.
+    u32 pv_grid() const { return (u32)rt.sms * (opt.pv_blocks > 0 ? (u32)opt.pv_blocks : 8u); }
 
     // prop (elimination.cpp:64-99).
     void prop() {
@@ -784,7 +791,7 @@ struct pf_sigma_ctx {
             a.work = work.p;
             a.nwork = nullptr;
             a.cap_work = (u32)work.n;
-            PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, loop_bound(), occ_x16()};
+            PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, loop_bound(), sweep_scale()};
             rt.zero(counters.p + 22, 5 * 4);  // [22..23] work counters, [24..25] barrier, [26] waves
             void* args[] = {&a, &w};
             rt.launches++;
@@ -814,7 +821,7 @@ struct pf_sigma_ctx {
             a.work = work.p;
             a.nwork = counters.p + 2;
             a.cap_work = (u32)work.n;
-            if (prop_use_sweep(pend, occ_x16(), ncls)) {
+            if (prop_use_sweep(pend, sweep_scale(), ncls)) {
                 rt.each(FPropSweep{a}, ncls);
                 rt.each(FPropSweepLists{a}, pend);
                 prop_head = ntrail;
@@ -985,7 +992,7 @@ struct pf_sigma_ctx {
         if (!perm_n) return;
         ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
         rt.launches++;
-        sub_warp_k<<<(u32)rt.sms * 8u, 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n, counters.p + 11);
+        sub_warp_k<<<pv_grid(), 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n, counters.p + 11);
         ck(cudaGetLastError(), "launch");
 #else
         pv_each(FSubWarp{a});
@@ -1243,7 +1250,7 @@ struct pf_sigma_ctx {
             ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
             rt.launches++;
             kclock[K_BVE].start(rt);
-            bve_warp_k<<<(u32)rt.sms * 8u, kBveWarpThreads, smem, rt.stream>>>(a, pv_perm.p, counters.p + 11);
+            bve_warp_k<<<pv_grid(), kBveWarpThreads, smem, rt.stream>>>(a, pv_perm.p, counters.p + 11);
             kclock[K_BVE].stop(rt);
             ck(cudaGetLastError(), "launch");
         }
@@ -1276,7 +1283,7 @@ struct pf_sigma_ctx {
         if (perm_n) {
             ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
             rt.launches++;
-            bve_write_warp_k<<<(u32)rt.sms * 8u, 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n,
+            bve_write_warp_k<<<pv_grid(), 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n,
                                                                        counters.p + 11);
             ck(cudaGetLastError(), "launch");
         }
@@ -1310,7 +1317,7 @@ struct pf_sigma_ctx {
         if (perm_n) {
             ck(cudaMemsetAsync(counters.p + 11, 0, 4, rt.stream), "memset");
             rt.launches++;
-            bce_count_warp_k<<<(u32)rt.sms * 8u, 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n, counters.p + 11);
+            bce_count_warp_k<<<pv_grid(), 256, 0, rt.stream>>>(a, pv_perm.p + perm_off, perm_n, counters.p + 11);
             ck(cudaGetLastError(), "launch");
         }
 #else

@@ -14,7 +14,8 @@ class PfOptions(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "phases", "all", "ve", "ve_plus", "sub", "bce", "ere", "ve_lbound", "ve_clause_max",
         "ve_phase_min", "mu_pos", "mu_neg", "xor_max_arity", "sub_max", "bce_max", "ere_max",
-        "ere_clause_max", "lcve_min", "gc_freq", "dump_level", "loop_limit", "proof", "ot_buckets")] + [("reserved", ctypes.c_int32 * 4)]
+        "ere_clause_max", "lcve_min", "gc_freq", "dump_level", "loop_limit", "proof", "ot_buckets", "sweep_div",
+        "pv_blocks")] + [("reserved", ctypes.c_int32 * 2)]
 
 
 # python field -> (reference option name, kind)
@@ -53,6 +54,8 @@ class Options:
     loop_limit: int = 0  # device-side loop rounds before PF_ETIMEOUT (0: variables + 2)
     proof: int = 0  # 1: record the round's DRAT proof (reference option "proof")
     ot_buckets: int = 0  # occurrence-table build: 0 by size, 1 literal buckets, -1 atomics
+    sweep_div: int = 0  # propagation sweeps when pending lists exceed 1/sweep_div of the store (0: 16, -1: never)
+    pv_blocks: int = 0  # blocks per SM of the per-variable warp kernels (0: 8)
 
     def derived(self) -> "Options":
         """Option derivation of the reference (src/cpu/options.cpp:281-311)."""
