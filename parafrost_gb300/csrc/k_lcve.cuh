@@ -167,6 +167,64 @@ HD void k_mis_rec(const LcveArgs& a, Q4* rec, u32 i) {
     spread_sum_add64(a.ws_bytes, (u64)ng * (4ull + (h_deleted(h.flags) ? 0ull : 8ull + 4ull * h.size)));
 }
 
+#if SIGMA_CUDA
+// k_mis_rec for 32 clauses per warp: lane i writes the record of clause id0 + i
+// (coalesced 16-byte stores), and the graph working set is summed over the warp's
+// literals with consecutive lanes on consecutive literals (coalesced reads), each
+// literal of a graph vertex adding 4 bytes and, in a live clause, the clause's
+// 8 + 4 * len bytes.
+__global__ void __launch_bounds__(256) mis_rec_warp_k(LcveArgs a, Q4* rec) {
+    const u32 lane = threadIdx.x & 31u;
+    const u32 nw = (gridDim.x * blockDim.x) >> 5;
+    const u32 ngroups = (a.c.ncls + 31u) / 32u;
+    u64 sum = 0;
+    for (u32 g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += nw) {
+        const u32 id0 = g * 32u;
+        const u32 n = a.c.ncls - id0 < 32u ? a.c.ncls - id0 : 32u;
+        u32 start = 0, sz = 0, weight = 0;
+        if (lane < n) {
+            const Hdr h = hdr_ro(&a.c.hdr[id0 + lane]);
+            const u32* l = a.c.lits + h.start;
+            Q4 q;
+            q.x = h.size > 0 ? __ldg(&l[0]) : 0u;
+            q.y = h.size > 1 ? __ldg(&l[1]) : 0u;
+            q.z = h.size > 2 ? __ldg(&l[2]) : 0u;
+            q.w = h.size | (h_deleted(h.flags) ? 0x80000000u : 0u);
+            rec[id0 + lane] = q;
+            start = h.start;
+            sz = h.size;
+            weight = 4u + (h_deleted(h.flags) ? 0u : 8u + 4u * h.size);
+        }
+        u32 incl = sz;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 t = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o) incl += t;
+        }
+        const u32 excl = incl - sz;
+        const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+        for (u32 base = 0; base < total; base += 32) {
+            const u32 j = base + lane;
+            u32 k = 0;
+#pragma unroll
+            for (u32 step = 16; step; step >>= 1) {
+                const u32 v = __shfl_sync(0xffffffffu, incl, k + step - 1);
+                if (v <= j) k += step;
+            }
+            const u32 st = __shfl_sync(0xffffffffu, start, k & 31u), ex = __shfl_sync(0xffffffffu, excl, k & 31u);
+            const u32 wt = __shfl_sync(0xffffffffu, weight, k & 31u);
+            if (j < total) {
+                const u32 x = ABS(__ldg(&a.c.lits[st + (j - ex)]));
+                if ((ldro(&a.gbits[x >> 5]) >> (x & 31u)) & 1u) sum += wt;
+            }
+        }
+    }
+    for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0 && sum) atomicAdd((unsigned long long*)(a.ws_bytes + (blockIdx.x & (kSpreadSlots - 1u))),
+                                    (unsigned long long)sum);
+}
+#endif
+
 // Whether clause cl holds a graph neighbour of v ranked below rv that is not out
 // (decisions are read through to the cache level other SMs write).
 HD bool mis_blocked_in(const LcveArgs& a, u32 v, u32 rv, const MisCl& cl) {

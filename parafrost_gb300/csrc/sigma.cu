@@ -890,7 +890,15 @@ struct pf_sigma_ctx {
         u32* ctr = counters.p + 12;  // [12..23] three sets of list lengths, [24..25] barrier, [26] rounds
         rt.zero(ctr, 15 * 4);
         rt.each(FMisInit{a, MisFront{flags.p, ctr, mis_big_a.p, ctr + 1}}, nvars + 1);
+#if SIGMA_CUDA
+        if (ncls) {
+            rt.launches++;
+            mis_rec_warp_k<<<rt.grid((ncls + 7u) / 8u, 8), 256, 0, rt.stream>>>(a, mis_rec.p);
+            ck(cudaGetLastError(), "launch");
+        }
+#else
         rt.each(FMisRec{a, mis_rec.p}, ncls);
+#endif
         u32 rounds = 0;
 #if SIGMA_CUDA
         MisRounds w;
