@@ -306,6 +306,7 @@ def run_ours(args) -> dict:
     clocks.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     stats = []
+    allocs0 = s.lib.pf_device_alloc_count()
     for i in range(args.steps):
         flush_l2(flush)
         ev[i][0].record()
@@ -313,6 +314,7 @@ def run_ours(args) -> dict:
         ev[i][1].record()
         stats.append(st)
     torch.cuda.synchronize()
+    allocs = s.lib.pf_device_alloc_count() - allocs0
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
@@ -393,6 +395,9 @@ def run_ours(args) -> dict:
                       "options": "-all, phases=5" + "".join(f", {k}={v}" for k, v in EXTRA_OPTS.items()),
                       "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
            "round_ms": round_ms, "stage_ms": stage_ms,
+           "step_ms": [round(x, 3) for x in step_ms], "round_ms_each": [round(x.ms_total, 3) for x in stats],
+           "device_allocs_per_step": allocs / args.steps,
+           "host_syncs_per_round": int(last.host_syncs), "prop_waves": int(last.prop_waves),
            "result": {"clauses_after": int(last.clauses_after), "phases": int(last.phases_run),
                       "status": int(last.status), "mis_rounds": int(last.mis_rounds),
                       "launches_per_round": int(last.kernel_launches)},

@@ -213,7 +213,16 @@ __global__ void __launch_bounds__(OTB_LIST_THREADS) ot_bucket_lists_k(OtbArgs a)
     for (u32 i = tid; i < nl; i += blockDim.x) otb_cnt[i] = 0;
     if (tid == 0) carry = 0;
     __syncthreads();
-    for (u32 k = p0 + tid; k < p1; k += blockDim.x) atomicAdd(&otb_cnt[(u32)__ldcg(&a.tpair[k]) - l0], 1u);
+    // four occurrences per thread per step, their loads issued before the atomics
+    const u32 step = 4u * blockDim.x;
+    for (u32 k0 = p0 + tid; k0 < p1; k0 += step) {
+        u64 x[4];
+#pragma unroll
+        for (u32 j = 0; j < 4; j++) x[j] = k0 + j * blockDim.x < p1 ? __ldcg(&a.tpair[k0 + j * blockDim.x]) : 0ull;
+#pragma unroll
+        for (u32 j = 0; j < 4; j++)
+            if (k0 + j * blockDim.x < p1) atomicAdd(&otb_cnt[(u32)x[j] - l0], 1u);
+    }
     __syncthreads();
     // block scan of the slot counts, blockDim.x slots per step: list sizes and starts
     for (u32 i0 = 0; i0 < nl; i0 += blockDim.x) {
@@ -239,9 +248,13 @@ __global__ void __launch_bounds__(OTB_LIST_THREADS) ot_bucket_lists_k(OtbArgs a)
         if (tid == blockDim.x - 1) carry = excl + v;
         __syncthreads();
     }
-    for (u32 k = p0 + tid; k < p1; k += blockDim.x) {
-        const u64 x = __ldcs(&a.tpair[k]);
-        a.c.ot_refs[p0 + atomicAdd(&otb_cnt[(u32)x - l0], 1u)] = (u32)(x >> 32);
+    for (u32 k0 = p0 + tid; k0 < p1; k0 += step) {
+        u64 x[4];
+#pragma unroll
+        for (u32 j = 0; j < 4; j++) x[j] = k0 + j * blockDim.x < p1 ? __ldcs(&a.tpair[k0 + j * blockDim.x]) : 0ull;
+#pragma unroll
+        for (u32 j = 0; j < 4; j++)
+            if (k0 + j * blockDim.x < p1) a.c.ot_refs[p0 + atomicAdd(&otb_cnt[(u32)x[j] - l0], 1u)] = (u32)(x[j] >> 32);
     }
 }
 
