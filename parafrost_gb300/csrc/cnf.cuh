@@ -133,6 +133,20 @@ HD void set_unsat(const Ctx& c, u32 v) {
 }
 HD u32 fid_of(const Ctx& c, u32 v) { return c.var_fid ? c.var_fid[v] : 0u; }
 
+// A unit found inside the round goes to the trail unless its variable is already
+// assigned; the opposite assignment is a conflict (enqueueUnit / learnEmpty paths of
+// bve.cpp:200-211, equivalence.h:56-80). The variable is claimed with a
+// compare-and-swap.
+HD void claim_unit(const Ctx& c, u32 u) {
+    const u32 old = atom_cas(&c.asg[ABS(u)], 0u, u);
+    if (old == 0) {
+        c.trail[atom_add(c.ntrail, 1u)] = u;
+        proof_line(c, &u, 1);  // learnUnit's proof.addUnit (src/cpu/solve.h:475-479)
+    } else if (old != u) {
+        set_unsat(c, ABS(u));
+    }
+}
+
 // Header load through the read-only path (for launches that write no header).
 HD Hdr hdr_ro(const Hdr* p) {
 #if defined(__CUDA_ARCH__)

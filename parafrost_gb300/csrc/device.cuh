@@ -395,8 +395,11 @@ DEV u64 global_ns() {
 }
 
 // Barrier over all blocks of a cooperative launch. A block whose wait runs out
-// records ERR_ITER and gets false (the launch then winds down).
-DEV bool grid_barrier(u32* bar, u32* err) {
+// records ERR_ITER and gets false (the launch then winds down). With snap_src, the
+// last block to arrive copies *snap_src to *snap_dst before it releases the others:
+// a counter that blocks advance between barriers, read at a moment when every block
+// is inside the barrier, so every block reads the same value after it.
+DEV bool grid_barrier(u32* bar, u32* err, const u32* snap_src = nullptr, u32* snap_dst = nullptr) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -404,6 +407,7 @@ DEV bool grid_barrier(u32* bar, u32* err) {
         const u32 gen = vload(&bar[1]);
         __threadfence();
         if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
+            if (snap_src) *(volatile u32*)snap_dst = vload(snap_src);
             atomicExch(&bar[0], 0u);
             __threadfence();
             atomicAdd(&bar[1], 1u);

@@ -201,19 +201,7 @@ HD u64 save_witness(const Ctx& c, u64 w, u32 lit) {
     return w;
 }
 
-// A unit found inside the round goes to the trail unless its variable is already
-// assigned; the opposite assignment is a conflict (enqueueUnit / learnEmpty paths of
-// bve.cpp:200-211, equivalence.h:56-80).
-HD void enqueue_unit(const Ctx& c, u32 u) {
-    const u32 old = atom_cas(&c.asg[ABS(u)], 0u, u);
-    if (old == 0) {
-        const u32 pos = atom_add(c.ntrail, 1u);
-        c.trail[pos] = u;
-        proof_line(c, &u, 1);  // learnUnit's proof.addUnit (src/cpu/solve.h:475-479)
-    } else if (old != u) {
-        set_unsat(c, ABS(u));
-    }
-}
+HD void enqueue_unit(const Ctx& c, u32 u) { claim_unit(c, u); }
 
 // toblivion(p, pOrgs, nOrgs, poss, negs, model) (simplify.h:305-332).
 HD void oblivion_var(const Ctx& c, u32 p, u32 pOrgs, u32 nOrgs, u64 w) {

@@ -337,6 +337,8 @@ struct MisRounds {
     u32* bar;        // grid barrier: [0] arrivals, [1] generation
     u32* rounds;     // out: rounds run
     u32 max_rounds;
+    u32* trace;      // optional: per round [undecided small, big, went-in small, big, start ns / 1024]
+    u32 trace_cap;   // rounds the trace holds
 };
 
 // Vertices leaving a pull phase are staged per block in shared memory and copied
@@ -425,6 +427,14 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
         }
         if (tid == 0)
             for (u32 k = 0; k < 4; k++) w.ctr[4 * old + k] = 0;
+        if (tid == 0 && w.trace && r < w.trace_cap) {
+            u32* t = w.trace + 5 * r;
+            t[0] = us;
+            t[1] = ub;
+            t[2] = is;
+            t[3] = ib;
+            t[4] = (u32)(global_ns() >> 10);
+        }
         // push: the vertices that went in last round (lists written by other blocks: uncached reads)
         const u32* pin_b = w.in_big[r & 1];
         for (u32 idx = tid >> 5; idx < ib; idx += nwarps) {

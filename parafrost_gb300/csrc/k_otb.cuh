@@ -28,8 +28,7 @@ namespace sigma {
 #if SIGMA_CUDA
 
 constexpr u32 OTB_TILE = 4096;      // clauses per block tile in pass 0
-constexpr u32 OTB_FILL_TILE = 1024;  // clauses per block tile in pass 1 (staged in shared memory)
-constexpr u32 OTB_FILL_CAP = 8192;   // staged occurrences per pass-1 step
+constexpr u32 OTB_FILL_CAP = 8192;   // occurrences of a pass-1 tile ordered in shared memory
 constexpr u32 OTB_MAX_BUCKETS = 4096;
 constexpr u32 OTB_MAX_SHIFT = 15;   // 32,768 slots: 128 KiB of shared counters in pass 2
 constexpr u32 OTB_LIST_THREADS = 512;
@@ -43,6 +42,7 @@ struct OtbArgs {
     u32* cursor;      // nb: next free position of every bucket (pass 1; starts at base)
     const u32* base;  // nb + 1: first position of every bucket, base[nb] = occurrences
     u64* tpair;       // occurrences grouped by bucket: clause id << 32 | literal
+    u32 fill_tile;    // clauses per pass-1 tile (a multiple of 32)
 };
 
 // The literals of the live clauses id0 .. id0+n-1 (n <= 32), walked by one warp with
@@ -131,42 +131,38 @@ DEV u32 otb_block_scan(u32* cnt, u32 n, u32* warp_tot, u32* carry) {
 }
 
 // Pass 1: occurrences grouped by bucket. A tile's occurrences are counted per
-// bucket and staged in shared memory in arrival order; one reservation per
-// non-empty bucket gives each run its place; the staged occurrences are ordered by
-// bucket (a block scan of the counts) and each run is written contiguously. A tile
-// with more occurrences than the stage holds (very long clauses) writes them to
-// their runs directly instead.
+// bucket (shared counters), one reservation per non-empty bucket gives each run its
+// place, a block scan of the counts orders the tile by bucket, and a second walk of
+// the tile's literals (just read, so mostly cache hits) places every occurrence in
+// shared memory at its bucket's position; the runs are then written out contiguously.
+// A tile with more occurrences than shared memory holds (very long clauses) writes
+// them to their runs directly instead. Tiles hold fill_tile clauses, sized from the
+// mean clause length so that a tile's occurrences nearly fill the stage.
 constexpr u32 OTB_FILL_THREADS = 512;
 __global__ void __launch_bounds__(OTB_FILL_THREADS) ot_bucket_fill_k(OtbArgs a) {
     extern __shared__ u64 otb_fsm[];
-    u64* stage = otb_fsm;                                           // OTB_FILL_CAP
-    u64* sorted = otb_fsm + OTB_FILL_CAP;                           // OTB_FILL_CAP
-    u32* cnt = reinterpret_cast<u32*>(otb_fsm + 2 * OTB_FILL_CAP);  // nb: counts, then tile offsets
-    u32* run = cnt + a.nb;                                          // nb: global start of the tile's run
-    u32* cur = run + a.nb;                                          // nb: cursors
+    u64* sorted = otb_fsm;                                      // OTB_FILL_CAP
+    u32* cnt = reinterpret_cast<u32*>(otb_fsm + OTB_FILL_CAP);  // nb: counts, then tile offsets
+    u32* run = cnt + a.nb;                                      // nb: global start of the tile's run
+    u32* cur = run + a.nb;                                      // nb: cursors
     __shared__ u32 warp_tot[OTB_FILL_THREADS / 32];
-    __shared__ u32 carry, nstage;
-    const u32 lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const u32 ntiles = (a.c.ncls + OTB_FILL_TILE - 1u) / OTB_FILL_TILE;
+    __shared__ u32 carry, ntile;
+    const u32 warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const u32 T = a.fill_tile;
+    const u32 ntiles = (a.c.ncls + T - 1u) / T;
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const u32 c0 = t * OTB_FILL_TILE, c1 = a.c.ncls - c0 < OTB_FILL_TILE ? a.c.ncls : c0 + OTB_FILL_TILE;
+        const u32 c0 = t * T, c1 = a.c.ncls - c0 < T ? a.c.ncls : c0 + T;
         for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) cnt[b] = 0;
-        if (threadIdx.x == 0) nstage = 0;
+        if (threadIdx.x == 0) ntile = 0;
         __syncthreads();
         for (u32 g = c0 + warp * 32u; g < c1; g += nw * 32u)
-            warp_clause_literals(a.c, g, c1 - g < 32u ? c1 - g : 32u, [&](bool valid, u32 lit, u32 cid) {
+            warp_clause_literals(a.c, g, c1 - g < 32u ? c1 - g : 32u, [&](bool valid, u32 lit, u32) {
                 const unsigned m = __ballot_sync(OTB_FULL, valid);
-                u32 base = 0;
-                if (lane == 0 && m) base = atomicAdd(&nstage, (u32)__popc(m));
-                base = __shfl_sync(OTB_FULL, base, 0);
-                if (valid) {
-                    const u32 pos = base + (u32)__popc(m & ((1u << lane) - 1u));
-                    if (pos < OTB_FILL_CAP) stage[pos] = ((u64)cid << 32) | lit;
-                    atomicAdd(&cnt[lit >> a.shift], 1u);
-                }
+                if ((threadIdx.x & 31u) == 0 && m) atomicAdd(&ntile, (u32)__popc(m));
+                if (valid) atomicAdd(&cnt[lit >> a.shift], 1u);
             });
         __syncthreads();
-        const u32 n = nstage;
+        const u32 n = ntile;
         for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) {
             const u32 k = cnt[b];
             run[b] = k ? atomicAdd(&a.cursor[b], k) : 0u;
@@ -175,10 +171,10 @@ __global__ void __launch_bounds__(OTB_FILL_THREADS) ot_bucket_fill_k(OtbArgs a) 
             otb_block_scan(cnt, a.nb, warp_tot, &carry);
             for (u32 b = threadIdx.x; b < a.nb; b += blockDim.x) cur[b] = cnt[b];
             __syncthreads();
-            for (u32 i = threadIdx.x; i < n; i += blockDim.x) {
-                const u64 x = stage[i];
-                sorted[atomicAdd(&cur[(u32)x >> a.shift], 1u)] = x;
-            }
+            for (u32 g = c0 + warp * 32u; g < c1; g += nw * 32u)
+                warp_clause_literals(a.c, g, c1 - g < 32u ? c1 - g : 32u, [&](bool valid, u32 lit, u32 cid) {
+                    if (valid) sorted[atomicAdd(&cur[lit >> a.shift], 1u)] = ((u64)cid << 32) | lit;
+                });
             __syncthreads();
             for (u32 i = threadIdx.x; i < n; i += blockDim.x) {
                 const u64 x = sorted[i];

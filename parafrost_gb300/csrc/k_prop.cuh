@@ -145,17 +145,7 @@ HD void prop_clause(const PropArgs& a, u32 k) {
         }
         return;
     }
-    if (n == 1) {
-        const u32 u = l[0];
-        const u32 old = atom_cas(&c.asg[ABS(u)], 0u, u);
-        if (old == 0) {
-            const u32 pos = atom_add(c.ntrail, 1u);
-            c.trail[pos] = u;
-            proof_line(c, &u, 1);  // learnUnit's proof.addUnit (src/cpu/solve.h:475-479)
-        } else if (old != u) {
-            set_unsat(c, ABS(u));
-        }
-    }
+    if (n == 1) claim_unit(c, l[0]);
 }
 
 HD void k_prop_lists(const PropArgs& a, u32 k) { prop_lists<false>(a, k); }
@@ -236,17 +226,7 @@ HD void prop_sweep_clause(const PropArgs& a, u32 r) {
         }
         return;
     }
-    if (n == 1) {
-        const u32 u = l[0];
-        const u32 old = atom_cas(&c.asg[ABS(u)], 0u, u);
-        if (old == 0) {
-            const u32 pos = atom_add(c.ntrail, 1u);
-            c.trail[pos] = u;
-            proof_line(c, &u, 1);
-        } else if (old != u) {
-            set_unsat(c, ABS(u));
-        }
-    }
+    if (n == 1) claim_unit(c, l[0]);
 }
 HD void k_prop_sweep(const PropArgs& a, u32 r) { prop_sweep_clause<false>(a, r); }
 // The lists of a swept wave's literals end empty, as the list waves leave them.
@@ -261,6 +241,83 @@ HD void k_prop_sweep_lists(const PropArgs& a, u32 k) {
 HD bool prop_use_sweep(u32 pending, u32 scale, u32 ncls) { return scale && (u64)pending * scale > (u64)ncls; }
 
 #if SIGMA_CUDA
+// prop_clause (Always) or prop_sweep_clause (not Always) for up to 32 clauses by one
+// warp: lane i loads the header of clause r (has: lane i holds one); the live
+// clauses' literals are then read and valued by consecutive lanes (32 literals of
+// the warp's clauses per step, all loads of a step in flight together), and lane i
+// learns from the step's ballots whether its clause has a true literal and how many
+// false ones. A clause with a true literal is deleted; otherwise its false literals
+// go (the clause is rewritten when it has some, or always for Always) as the
+// per-thread versions do, whose results these are.
+template <bool Always>
+DEV void prop_warp_clauses(const PropArgs& a, u32 r, bool has) {
+    const Ctx& c = a.c;
+    const u32 lane = threadIdx.x & 31u;
+    Hdr h;
+    h.start = h.size = h.sig = h.flags = 0;
+    if (has) h = ldw_hdr<true>(&c.hdr[r]);
+    const bool live = has && !h_deleted(h.flags);
+    const u32 sz = live ? h.size : 0u;
+    u32 incl = sz;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 t = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane >= o) incl += t;
+    }
+    const u32 excl = incl - sz;
+    const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+    bool sat = false;
+    u32 nfalse = 0;
+    for (u32 base = 0; base < total; base += 32) {
+        const u32 j = base + lane;
+        u32 k = 0;  // the lane whose clause holds literal j: the first with incl > j
+#pragma unroll
+        for (u32 step = 16; step; step >>= 1) {
+            const u32 v = __shfl_sync(0xffffffffu, incl, k + step - 1);
+            if (v <= j) k += step;
+        }
+        const u32 st = __shfl_sync(0xffffffffu, h.start, k & 31u), ex = __shfl_sync(0xffffffffu, excl, k & 31u);
+        const int val = j < total ? lit_value(c, ldw<true>(&c.lits[st + (j - ex)])) : VAL_UNDEF;
+        const u32 bt = __ballot_sync(0xffffffffu, val == 1), bf = __ballot_sync(0xffffffffu, val == 0);
+        // this lane's literals in the step: [excl - base, incl - base) clipped to the warp
+        const int lo = max((int)excl - (int)base, 0), hi = min((int)incl - (int)base, 32);
+        if (lo < hi) {
+            const u32 m = (hi - lo == 32 ? 0xffffffffu : ((1u << (hi - lo)) - 1u)) << lo;
+            sat |= (bt & m) != 0;
+            nfalse += (u32)__popc(bf & m);
+        }
+    }
+    if (!live) return;
+    if (sat) {
+        c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+        touch(c, r);
+        return;
+    }
+    if (!Always && !nfalse) return;
+    u32* l = c.lits + h.start;
+    const u32 v0 = ABS(ldw<true>(&l[0]));  // names the formula if the clause empties
+    u32 n = 0, sig = 0;
+    for (u32 i = 0; i < h.size; i++) {
+        const u32 lit = ldw<true>(&l[i]);
+        if (lit_value(c, lit) == 0) continue;
+        l[n++] = lit;
+        sig |= MAPHASH(lit);
+    }
+    h.size = n;
+    h.sig = sig;
+    c.hdr[r] = h;
+    touch(c, r);
+    if (n == 0) {
+        set_unsat(c, v0);
+        if (c.var_fid) {
+            c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
+            touch(c, r);
+        }
+        return;
+    }
+    if (n == 1) claim_unit(c, l[0]);
+}
+
 // Every wave of one propagation in one cooperative launch: wave A over the trail
 // literals [head, tail), a grid barrier, wave B over the collected clauses, a
 // barrier, then the literals wave B appended. Wave w uses work counter w & 1 and
@@ -271,13 +328,19 @@ struct PropWaves {
     u32* waves;      // out: waves run
     u32 max_waves;
     u32 sweep_scale; // mean occurrences per literal x sweep divisor (0: never sweep)
+    u32* trace;      // optional: per wave [pending, collected | sweep << 31, start, clause pass start (ns / 1024)]
+    u32 trace_cap;   // waves the trace holds
+    u32* tail;       // the trail length every block uses for the wave (set before the
+                     // launch and by the barrier that ends each wave)
 };
 
 __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
     const u32 tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     u32 head = a.head;
     for (u32 wave = 0;; wave++) {
-        const u32 tail = vload(a.c.ntrail);
+        // a sweep claims units while slower blocks may still be starting the wave, so
+        // the wave's end of the trail is the copy the last barrier took
+        const u32 tail = vload(w.tail);
         if (tail == head) {
             if (tid == 0) *w.waves = wave;
             return;
@@ -291,20 +354,37 @@ __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
         b.stamp = a.stamp + wave;
         b.nwork = &w.nwork2[wave & 1];
         if (tid == 0) w.nwork2[(wave + 1) & 1] = 0;
-        if (prop_use_sweep(tail - head, w.sweep_scale, a.c.ncls)) {
-            for (u32 r = tid; r < a.c.ncls; r += nth) prop_sweep_clause<true>(b, r);
+        const bool sweep = prop_use_sweep(tail - head, w.sweep_scale, a.c.ncls);
+        if (tid == 0 && w.trace && wave < w.trace_cap) {
+            w.trace[4 * wave] = tail - head;
+            w.trace[4 * wave + 1] = sweep ? 1u << 31 : 0u;
+            w.trace[4 * wave + 2] = (u32)(global_ns() >> 10);
+            w.trace[4 * wave + 3] = 0;
+        }
+        const u32 warp = tid >> 5, nwarps = nth >> 5;
+        if (sweep) {
+            for (u32 g = warp; g < (a.c.ncls + 31u) / 32u; g += nwarps) {
+                const u32 r = g * 32u + (tid & 31u);
+                prop_warp_clauses<false>(b, r, r < a.c.ncls);
+            }
             for (u32 i = tid; i < tail - head; i += nth) k_prop_sweep_lists(b, i);
-            if (!grid_barrier(w.bar, a.c.err)) return;
+            if (!grid_barrier(w.bar, a.c.err, a.c.ntrail, w.tail)) return;
             head = tail;
             continue;
         }
-        const u32 nwarps = nth >> 5;
-        for (u32 i = tid >> 5; i < tail - head; i += nwarps) prop_lists_warp(b, i);
+        for (u32 i = warp; i < tail - head; i += nwarps) prop_lists_warp(b, i);
         if (!grid_barrier(w.bar, a.c.err)) return;
         const u32 n = vload(b.nwork);
         const u32 nw = n < a.cap_work ? n : a.cap_work;
-        for (u32 i = tid; i < nw; i += nth) prop_clause<true>(b, i);
-        if (!grid_barrier(w.bar, a.c.err)) return;
+        if (tid == 0 && w.trace && wave < w.trace_cap) {
+            w.trace[4 * wave + 1] = n;
+            w.trace[4 * wave + 3] = (u32)(global_ns() >> 10);
+        }
+        for (u32 g = warp; g < (nw + 31u) / 32u; g += nwarps) {
+            const u32 k = g * 32u + (tid & 31u);
+            prop_warp_clauses<true>(b, k < nw ? __ldcg(&b.work[k]) : 0u, k < nw);
+        }
+        if (!grid_barrier(w.bar, a.c.err, a.c.ntrail, w.tail)) return;
         head = tail;
     }
 }

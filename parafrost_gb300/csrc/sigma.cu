@@ -695,15 +695,18 @@ struct pf_sigma_ctx {
         otb_cursor.reserve(rt, nb + 1);
         otb_pair.reserve(rt, (size_t)nlits_used + 1);
         rt.zero(otb_count.p, (size_t)nb * 4);
-        OtbArgs a{view(), shift, nb, otb_count.p, otb_cursor.p, otb_base.p, otb_pair.p};
-        const u32 fill_smem = 2 * OTB_FILL_CAP * 8 + 3 * nb * 4;
+        // pass-1 tiles: about 7/8 of the stage at the store's mean clause length
+        const u64 mean_x8 = std::max<u64>(8ull * nlits_used / std::max<u32>(ncls, 1), 8);
+        const u32 fill_tile = (u32)std::min<u64>(std::max<u64>(7ull * OTB_FILL_CAP / mean_x8, 32), 4096) & ~31u;
+        OtbArgs a{view(), shift, nb, otb_count.p, otb_cursor.p, otb_base.p, otb_pair.p, fill_tile};
+        const u32 fill_smem = OTB_FILL_CAP * 8 + 3 * nb * 4;
         static bool attr_set = false;
         if (!attr_set) {
             ck(cudaFuncSetAttribute(ot_bucket_lists_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)((1u << OTB_MAX_SHIFT) * 4)),
                "smem attr");
             ck(cudaFuncSetAttribute(ot_bucket_fill_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(2 * OTB_FILL_CAP * 8 + 3 * OTB_MAX_BUCKETS * 4)),
+                                    (int)(OTB_FILL_CAP * 8 + 3 * OTB_MAX_BUCKETS * 4)),
                "smem attr");
             attr_set = true;
         }
@@ -715,7 +718,7 @@ struct pf_sigma_ctx {
         }
         scan1_launch(otb_count.p, otb_base.p, nb, otb_base.p + nb);
         rt.d2d(otb_cursor.p, otb_base.p, (size_t)nb * 4);
-        const u32 ntiles = (ncls + OTB_FILL_TILE - 1) / OTB_FILL_TILE;
+        const u32 ntiles = (ncls + fill_tile - 1) / fill_tile;
         if (ntiles) {
             rt.launches++;
             ot_bucket_fill_k<<<std::min((u32)rt.sms * 2u, ntiles), OTB_FILL_THREADS, fill_smem, rt.stream>>>(a);
@@ -772,6 +775,44 @@ struct pf_sigma_ctx {
     // Blocks of the per-variable warp kernels.
     u32 pv_grid() const { return (u32)rt.sms * (opt.pv_blocks > 0 ? (u32)opt.pv_blocks : 8u); }
 
+#if SIGMA_CUDA
+    // Traces of the persistent launches, printed to stderr when the environment sets
+    // PF_TRACE: per propagation wave the pending literals, the clauses collected (or
+    // "sweep") and the wave's device time; per election round the undecided and
+    // went-in vertex lists (small and big adjacency) and the round's device time.
+    static constexpr u32 kPropTraceWaves = 4096;
+    const bool trace_on = std::getenv("PF_TRACE") != nullptr;
+    DBuf<u32> prop_trace;
+    void print_mis_trace(u32 rounds) {
+        const u32 n = std::min(rounds, kPropTraceWaves);
+        std::vector<u32> t(5 * (size_t)n + 5);
+        if (n) rt.d2h(t.data(), prop_trace.p, 5 * (size_t)n * 4);
+        std::fprintf(stderr, "election phase %u: %u rounds\n", phase, rounds);
+        for (u32 i = 0; i < n; i++) {
+            const double us = i + 1 < n ? (double)(u32)(t[5 * i + 9] - t[5 * i + 4]) * 1.024 : 0.0;
+            std::fprintf(stderr, "  round %u undecided %u+%u in %u+%u %.1f us\n", i, t[5 * i], t[5 * i + 1],
+                         t[5 * i + 2], t[5 * i + 3], us);
+        }
+    }
+    void print_prop_trace(u32 waves) {
+        const u32 n = std::min(waves, kPropTraceWaves);
+        std::vector<u32> t(4 * (size_t)n + 4);
+        if (n) rt.d2h(t.data(), prop_trace.p, 4 * (size_t)n * 4);
+        std::fprintf(stderr, "prop phase %u: %u waves, ncls %u\n", phase, waves, ncls);
+        for (u32 i = 0; i < n; i++) {
+            const u32* w = &t[4 * i];
+            const double us = i + 1 < n ? (double)(u32)(w[6] - w[2]) * 1.024 : 0.0;
+            if (w[1] >> 31) {
+                std::fprintf(stderr, "  wave %u pending %u sweep %.1f us\n", i, w[0], us);
+            } else {
+                const double la = w[3] ? (double)(u32)(w[3] - w[2]) * 1.024 : 0.0;
+                std::fprintf(stderr, "  wave %u pending %u collected %u %.1f us (lists %.1f us)\n", i, w[0], w[1], us,
+                             la);
+            }
+        }
+    }
+#endif
+
     // prop (elimination.cpp:64-99).
     void prop() {
         if (prop_head >= ntrail) return;
@@ -791,8 +832,15 @@ struct pf_sigma_ctx {
             a.work = work.p;
             a.nwork = nullptr;
             a.cap_work = (u32)work.n;
-            PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, loop_bound(), sweep_scale()};
+            PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, loop_bound(), sweep_scale(),
+                        nullptr, 0, counters.p + 28};
+            if (trace_on) {
+                prop_trace.reserve(rt, 5 * kPropTraceWaves);
+                w.trace = prop_trace.p;
+                w.trace_cap = kPropTraceWaves - 1;
+            }
             rt.zero(counters.p + 22, 5 * 4);  // [22..23] work counters, [24..25] barrier, [26] waves
+            rt.d2d(counters.p + 28, counters.p + 0, 4);  // [28] the trail's end for the first wave
             void* args[] = {&a, &w};
             rt.launches++;
             // four blocks per SM: most waves of a propagation are small, and the grid
@@ -802,6 +850,7 @@ struct pf_sigma_ctx {
                "cooperative launch");
             check();
             const u32 waves = read_u32(counters.p + 26);
+            if (trace_on) print_prop_trace(waves);
             wave_stamp += waves;
             prop_waves += waves;
             ntrail = read_u32(counters.p + 0);
@@ -914,6 +963,13 @@ struct pf_sigma_ctx {
         w.bar = ctr + 12;
         w.rounds = ctr + 14;
         w.max_rounds = loop_bound();
+        w.trace = nullptr;
+        w.trace_cap = 0;
+        if (trace_on) {
+            prop_trace.reserve(rt, 5 * kPropTraceWaves);
+            w.trace = prop_trace.p;
+            w.trace_cap = kPropTraceWaves;
+        }
         void* args[] = {&a, &w};
         kclock[K_MIS].start(rt);
         ck(cudaLaunchCooperativeKernel((const void*)mis_rounds_k, dim3(mis_rounds_grid()), dim3(256), args, 0,
@@ -953,6 +1009,7 @@ struct pf_sigma_ctx {
         npvs = (u32)hr[0];
 #if SIGMA_CUDA
         rounds = (u32)hr[1];
+        if (trace_on) print_mis_trace(rounds);
 #endif
         mis_rounds += rounds;
         rt.each(FElectWrite{a, flags.p, flags_scan.p}, nvars);
@@ -2706,6 +2763,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     c.otb_base.free();
     c.otb_cursor.free();
     c.otb_pair.free();
+    c.prop_trace.free();
 #endif
     c.pv_perm.free();
     c.pv_key.free();
