@@ -151,33 +151,80 @@ HD void prop_clause(const PropArgs& a, u32 k) {
 HD void k_prop_lists(const PropArgs& a, u32 k) { prop_lists<false>(a, k); }
 
 #if SIGMA_CUDA
-// Wave A with one warp per pending literal (lanes take the list entries), so a
-// long list is never one thread's critical path.
-DEV void prop_lists_warp(const PropArgs& a, u32 k) {
+// A warp's run of reserved work-list slots [at, end) (the same in every lane). The
+// collected clauses go to the run; a run that cannot take a step's clauses is
+// closed (its free slots hold NONE, which the clause pass skips) and a new run of
+// PROP_SLOTS is reserved, so the list's counter takes one atomic per run rather
+// than one per step of every warp.
+constexpr u32 PROP_SLOTS = 256;
+struct WarpSlots {
+    u32 at = 0, end = 0;
+};
+DEV void slots_close(const PropArgs& a, WarpSlots& ws) {
+    for (u32 i = ws.at + (threadIdx.x & 31u); i < ws.end; i += 32)
+        if (i < a.cap_work) a.work[i] = NONE;
+    ws.at = ws.end = 0;
+}
+DEV u32 slots_append(const PropArgs& a, WarpSlots& ws, bool pred) {
+    const u32 lane = threadIdx.x & 31u;
+    const u32 m = __ballot_sync(0xffffffffu, pred);
+    if (!m) return 0;
+    const u32 cnt = (u32)__popc(m);
+    if (ws.at + cnt > ws.end) {
+        slots_close(a, ws);
+        u32 nb = 0;
+        if (lane == 0) nb = atomicAdd(a.nwork, PROP_SLOTS);
+        nb = __shfl_sync(0xffffffffu, nb, 0);
+        ws.at = nb;
+        ws.end = nb + PROP_SLOTS;
+    }
+    const u32 pos = ws.at + (u32)__popc(m & ((1u << lane) - 1u));
+    ws.at += cnt;
+    return pos;
+}
+
+// Wave A by warps over one pending literal's two lists seen as one range: entries
+// [0, fs) collect ot[-t], entries [fs, fs + ts) delete the clauses of ot[t]. A warp
+// takes entries [s0, s1) of pending literal k, lanes on consecutive entries. The
+// lists are emptied by the wave's clause pass, once every part has been walked.
+DEV void prop_lists_part(const PropArgs& a, WarpSlots& ws, u32 k, u32 s0, u32 s1) {
     const Ctx& c = a.c;
     const u32 lane = threadIdx.x & 31u;
     const u32 t = __ldcg(&c.trail[a.head + k]);
     const u32 f = FLIP(t);
     const u32 fo = c.ot_off[f], fs = __ldcg(&c.ot_size[f]);
-    const u32 to = c.ot_off[t], ts = __ldcg(&c.ot_size[t]);
-    for (u32 i = lane; i < fs; i += 32) {
-        const u32 r = c.ot_refs[fo + i];
-        const bool take = !h_deleted(__ldcg(&c.hdr[r].flags)) && atomicExch(&a.cl_stamp[r], a.stamp) != a.stamp;
-        const u32 pos = warp_append(a.nwork, take);
+    const u32 to = c.ot_off[t];
+    const u32 e = s1 < fs ? s1 : fs;
+    for (u32 i0 = s0; i0 < e; i0 += 32) {
+        const u32 i = i0 + lane;
+        const u32 r = i < e ? c.ot_refs[fo + i] : 0u;
+        const bool take = i < e && !h_deleted(__ldcg(&c.hdr[r].flags)) && atomicExch(&a.cl_stamp[r], a.stamp) != a.stamp;
+        const u32 pos = slots_append(a, ws, take);
         if (!take) continue;
         if (pos < a.cap_work) a.work[pos] = r;
         else set_err(c, ERR_CAP_SCRATCH);
     }
-    for (u32 i = lane; i < ts; i += 32) {
-        const u32 r = c.ot_refs[to + i];
+    for (u32 i = (s0 > fs ? s0 : fs) + lane; i < s1; i += 32) {
+        const u32 r = c.ot_refs[to + (i - fs)];
         c.hdr[r].flags = (__ldcg(&c.hdr[r].flags) & ~3u) | ST_DELETED;
         touch(c, r);
     }
-    __syncwarp();
-    if (lane == 0) {
-        c.ot_size[t] = 0;
-        c.ot_size[f] = 0;
+}
+// Pending literal k by one warp: its first PROP_PART entries here, the rest as parts
+// of PROP_PART entries on the part list, walked by all warps after the wave's
+// first barrier (one long list is then never one warp's critical path).
+constexpr u32 PROP_PART = 2048;
+DEV void prop_lists_warp(const PropArgs& a, WarpSlots& ws, u32 k, u64* parts, u32* nparts, u32 cap_parts) {
+    const Ctx& c = a.c;
+    const u32 lane = threadIdx.x & 31u;
+    const u32 t = __ldcg(&c.trail[a.head + k]);
+    const u32 n = __ldcg(&c.ot_size[FLIP(t)]) + __ldcg(&c.ot_size[t]);
+    for (u32 s0 = PROP_PART * (lane + 1u); s0 < n; s0 += 32u * PROP_PART) {
+        const u32 q = atomicAdd(nparts, 1u);
+        if (q < cap_parts) parts[q] = (u64)k << 32 | s0;
+        else set_err(c, ERR_CAP_SCRATCH);
     }
+    prop_lists_part(a, ws, k, 0, n < PROP_PART ? n : PROP_PART);
 }
 #endif
 HD void k_prop_clause(const PropArgs& a, u32 k) { prop_clause<false>(a, k); }
@@ -332,6 +379,9 @@ struct PropWaves {
     u32 trace_cap;   // waves the trace holds
     u32* tail;       // the trail length every block uses for the wave (set before the
                      // launch and by the barrier that ends each wave)
+    u64* parts;      // list parts past a pending literal's first PROP_PART entries:
+    u32* nparts2;    // pending index << 32 | first entry; two counters (wave & 1)
+    u32 cap_parts;
 };
 
 __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
@@ -353,7 +403,10 @@ __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
         b.head = head;
         b.stamp = a.stamp + wave;
         b.nwork = &w.nwork2[wave & 1];
-        if (tid == 0) w.nwork2[(wave + 1) & 1] = 0;
+        if (tid == 0) {
+            w.nwork2[(wave + 1) & 1] = 0;
+            w.nparts2[(wave + 1) & 1] = 0;
+        }
         const bool sweep = prop_use_sweep(tail - head, w.sweep_scale, a.c.ncls);
         if (tid == 0 && w.trace && wave < w.trace_cap) {
             w.trace[4 * wave] = tail - head;
@@ -372,8 +425,24 @@ __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
             head = tail;
             continue;
         }
-        for (u32 i = warp; i < tail - head; i += nwarps) prop_lists_warp(b, i);
+        u32* nparts = &w.nparts2[wave & 1];
+        WarpSlots ws;
+        for (u32 i = warp; i < tail - head; i += nwarps) prop_lists_warp(b, ws, i, w.parts, nparts, w.cap_parts);
+        slots_close(b, ws);
         if (!grid_barrier(w.bar, a.c.err)) return;
+        const u32 np = vload(nparts);
+        if (np) {
+            const u32 npc = np < w.cap_parts ? np : w.cap_parts;
+            for (u32 i = warp; i < npc; i += nwarps) {
+                const u64 q = __ldcg(&w.parts[i]);
+                const u32 k = (u32)(q >> 32), s0 = (u32)q;
+                const u32 t = __ldcg(&a.c.trail[head + k]);
+                const u32 n = __ldcg(&a.c.ot_size[FLIP(t)]) + __ldcg(&a.c.ot_size[t]);
+                prop_lists_part(b, ws, k, s0, n - s0 < PROP_PART ? n : s0 + PROP_PART);
+            }
+            slots_close(b, ws);
+            if (!grid_barrier(w.bar, a.c.err)) return;
+        }
         const u32 n = vload(b.nwork);
         const u32 nw = n < a.cap_work ? n : a.cap_work;
         if (tid == 0 && w.trace && wave < w.trace_cap) {
@@ -382,8 +451,10 @@ __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
         }
         for (u32 g = warp; g < (nw + 31u) / 32u; g += nwarps) {
             const u32 k = g * 32u + (tid & 31u);
-            prop_warp_clauses<true>(b, k < nw ? __ldcg(&b.work[k]) : 0u, k < nw);
+            const u32 r = k < nw ? __ldcg(&b.work[k]) : NONE;  // NONE: a free slot of a closed run
+            prop_warp_clauses<true>(b, r, r != NONE);
         }
+        for (u32 i = tid; i < tail - head; i += nth) k_prop_sweep_lists(b, i);
         if (!grid_barrier(w.bar, a.c.err, a.c.ntrail, w.tail)) return;
         head = tail;
     }

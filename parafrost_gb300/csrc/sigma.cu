@@ -348,6 +348,8 @@ struct pf_sigma_ctx {
     DBuf<u64> scan_tmp64;
     DBuf<u64> big64a, big64b;
     DBuf<uint8_t> down_learnt;  // learnt flags of the downloaded clauses
+    DBuf<u64> up_off;           // offsets of an upload from host buffers
+    DBuf<uint8_t> up_learnt;    // learnt flags of an upload from host buffers
     DBuf<u32> big32a, big32b;
     // BVE
     DBuf<uint8_t> ve_type;
@@ -783,6 +785,7 @@ struct pf_sigma_ctx {
     static constexpr u32 kPropTraceWaves = 4096;
     const bool trace_on = std::getenv("PF_TRACE") != nullptr;
     DBuf<u32> prop_trace;
+    DBuf<u64> prop_parts;
     void print_mis_trace(u32 rounds) {
         const u32 n = std::min(rounds, kPropTraceWaves);
         std::vector<u32> t(5 * (size_t)n + 5);
@@ -816,7 +819,14 @@ struct pf_sigma_ctx {
     // prop (elimination.cpp:64-99).
     void prop() {
         if (prop_head >= ntrail) return;
+#if SIGMA_CUDA
+        // collected clauses plus the free slots of the warps' closed runs (at most 31
+        // per run of PROP_SLOTS, and two partly used runs per warp and wave)
+        const size_t nwarps = (size_t)rt.sms * 4 * 256 / 32;
+        work.reserve(rt, (size_t)ot_refs.n + ot_refs.n / 8 + 2 * nwarps * PROP_SLOTS + 1024);
+#else
         work.reserve(rt, (size_t)std::max<u64>(ot_refs.n, 1024));
+#endif
         if (cl_stamp.n < hdr.n) {
             cl_stamp.reserve(rt, hdr.n);
             rt.zero(cl_stamp.p, cl_stamp.bytes());
@@ -832,8 +842,10 @@ struct pf_sigma_ctx {
             a.work = work.p;
             a.nwork = nullptr;
             a.cap_work = (u32)work.n;
+            // parts of long lists: at most one per PROP_PART occurrences of the table
+            prop_parts.reserve(rt, (size_t)(nlits_used / PROP_PART) + 1024);
             PropWaves w{counters.p + 22, counters.p + 24, counters.p + 26, loop_bound(), sweep_scale(),
-                        nullptr, 0, counters.p + 28};
+                        nullptr, 0, counters.p + 28, prop_parts.p, counters.p + 29, (u32)prop_parts.n};
             if (trace_on) {
                 prop_trace.reserve(rt, 5 * kPropTraceWaves);
                 w.trace = prop_trace.p;
@@ -841,6 +853,7 @@ struct pf_sigma_ctx {
             }
             rt.zero(counters.p + 22, 5 * 4);  // [22..23] work counters, [24..25] barrier, [26] waves
             rt.d2d(counters.p + 28, counters.p + 0, 4);  // [28] the trail's end for the first wave
+            rt.zero(counters.p + 29, 2 * 4);             // [29..30] list-part counters
             void* args[] = {&a, &w};
             rt.launches++;
             // four blocks per SM: most waves of a propagation are small, and the grid
@@ -1516,11 +1529,19 @@ struct pf_sigma_ctx {
         compact = true;
     }
 
-    // resizeCNF (solve.h:684-688).
+    // resizeCNF (solve.h:684-688). Besides the reference's schedule, a large store
+    // whose live clauses fill less than a quarter of its slots is compacted too: the
+    // compaction keeps the clauses' order, so no result of the round changes, and the
+    // next phase's passes over the store (table build, sweeps, clause records) stop
+    // walking dead slots. Not while stage dumps are written (they name clauses by
+    // their place in the store).
     void resize_cnf() {
         const int times = phase + 1;
-        if (opt.gc_freq > 0 && times > 1 && times != opt.phases && (times % opt.gc_freq) == 0) gc();
+        const bool sched = opt.gc_freq > 0 && times > 1 && times != opt.phases && (times % opt.gc_freq) == 0;
+        const bool sparse = opt.dump_level == 0 && ncls >= kSparseGcMin && (u64)n_cls_after * 4 < ncls;
+        if (sched || sparse) gc();
     }
+    static constexpr u32 kSparseGcMin = 1u << 20;
 
     // Rounds a device-side loop may run (election rounds, propagation waves).
     u32 loop_bound() const { return opt.loop_limit > 0 ? (u32)opt.loop_limit : nvars + 2; }
@@ -2163,8 +2184,10 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         rt.zero(c.counters.p, 32 * 4);
         rt.zero(c.counters64.p, 8 * 8);
         // literals and offsets
-        DBuf<u64> doff;
-        DBuf<uint8_t> dlearnt;
+        // offsets and learnt flags from host buffers land in buffers the context keeps
+        // (an upload of the same size allocates nothing)
+        DBuf<u64>& doff = c.up_off;
+        DBuf<uint8_t>& dlearnt = c.up_learnt;
         const u64* off_ptr = offsets;
         const uint8_t* learnt_ptr = learnt;
         if (parts) {
@@ -2243,8 +2266,6 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         }
         rt.each(FUpload{a}, (u32)num_clauses);
         rt.sync();
-        doff.free();
-        dlearnt.free();
         dcls.free();
         dnv.free();
         const u32 e = c.read_err();
@@ -2748,6 +2769,8 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     c.mis_rec.free();
     c.mis_gbits.free();
     c.down_learnt.free();
+    c.up_off.free();
+    c.up_learnt.free();
     c.res_mark.free();
 #if SIGMA_CUDA
     c.scan1_agg.free();
@@ -2764,6 +2787,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     c.otb_cursor.free();
     c.otb_pair.free();
     c.prop_trace.free();
+    c.prop_parts.free();
 #endif
     c.pv_perm.free();
     c.pv_key.free();
