@@ -19,17 +19,17 @@
 
 namespace sigma {
 
-// Independent-set word of a variable (one 64-bit word, so a neighbour test reads
-// one sector): bits 0-31 the variable's rank if it is a vertex of the graph (NONE
-// otherwise; never changes while the set is decided), bits 32-61 where the
-// vertex's last pull walk stopped (an index into its two lists), bits 62-63 the
-// decision.
+// Independent-set word of a variable, read by every neighbour test: bits 0-29 the
+// variable's rank if it is a vertex of the graph (MIS_NO_RANK otherwise; never
+// changes while the set is decided), bits 30-31 the decision. Four bytes a
+// variable keep the words of a 20M-variable graph (80 MB) in L2 while the walks
+// stream clause records past them. Where a vertex's last pull walk stopped (an
+// index into its two lists) is a separate word that only the vertex's walk reads.
 enum : u32 { MIS_UNDECIDED = 0, MIS_IN = 1, MIS_OUT = 2 };
-HD u32 mis_rank(u64 w) { return (u32)w; }
-HD u32 mis_resume(u64 w) { return (u32)(w >> 32) & 0x3FFFFFFFu; }
-HD u64 mis_with_resume(u32 rank, u32 pos) { return (u64)rank | ((u64)pos << 32); }
-HD u32 mis_dec(u64 w) { return (u32)(w >> 62); }
-HD u64 mis_dec_bits(u32 d) { return (u64)d << 62; }
+constexpr u32 MIS_NO_RANK = 0x3FFFFFFFu;
+HD u32 mis_rank(u32 w) { return w & MIS_NO_RANK; }
+HD u32 mis_dec(u32 w) { return w >> 30; }
+HD u32 mis_dec_bits(u32 d) { return d << 30; }
 
 struct LcveArgs {
     Ctx c;
@@ -37,7 +37,8 @@ struct LcveArgs {
     u32* score;           // nvars+1
     u32* order;           // nvars: variables in (score, var) order
     u32* rank;            // nvars+1
-    u64* word;            // nvars+1: independent-set words
+    u32* word;            // nvars+1: independent-set words
+    u32* resume;          // nvars+1: where each vertex's last pull walk stopped
     const Q4* crec;       // per clause: its first three literals and size | deleted << 31
     u64* ws_bytes;        // kSpreadSlots words summing the graph's working set (4*occ + sum(8 + 4*len))
     u32* gbits;           // graph membership, one bit per variable (zeroed before k_mis_init)
@@ -112,7 +113,8 @@ HD void k_mis_init(const LcveArgs& a, const MisFront& und, u32 v) {
     const u32 f = v ? fid_of(a.c, v) : 0u;
     const bool in_graph = v && (!a.f_active || a.f_active[f]) && lcve_valid(a.c, v) && lcve_freezable(a, v) &&
                           a.rank[v] < a.bound[2 * f];
-    a.word[v] = in_graph ? a.rank[v] : NONE;
+    a.word[v] = in_graph ? a.rank[v] : MIS_NO_RANK;
+    a.resume[v] = 0;
     bitmap_set(a.gbits, v, in_graph);
     mis_append(und, a.c, v, in_graph);
 }
@@ -239,7 +241,7 @@ HD bool mis_blocked_in(const LcveArgs& a, u32 v, u32 rv, const MisCl& cl) {
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) {
             if (w[j] == v) continue;
-            const u64 g = vload64(&a.word[w[j]]);
+            const u32 g = vload(&a.word[w[j]]);
             b |= mis_rank(g) < rv && mis_dec(g) != MIS_OUT;
         }
         if (b) return true;
@@ -250,24 +252,24 @@ HD bool mis_blocked_in(const LcveArgs& a, u32 v, u32 rv, const MisCl& cl) {
 // Pull walk of undecided vertex v by one thread: true when v went in; otherwise the
 // resume point is stored (v stays undecided). The next clause's record is loaded
 // before the current one is examined.
-HD bool mis_pull_one(const LcveArgs& a, u32 v, u64 wv) {
+HD bool mis_pull_one(const LcveArgs& a, u32 v, u32 wv) {
     const u32 rv = mis_rank(wv);
     const u32 p = V2L(v), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
     const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
-    u32 t = mis_resume(wv);
+    u32 t = vload(&a.resume[v]);
     if (t < n) {
         MisCl cl = mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + t]));
         for (; t < n; t++) {
             MisCl nx = cl;
             if (t + 1 < n) nx = mis_cl(a, ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1]));
             if (mis_blocked_in(a, v, rv, cl)) {
-                a.word[v] = mis_with_resume(rv, t);
+                a.resume[v] = t;
                 return false;
             }
             cl = nx;
         }
     }
-    atom_or64(&a.word[v], mis_dec_bits(MIS_IN));
+    atom_or(&a.word[v], mis_dec_bits(MIS_IN));
     return true;
 }
 
@@ -285,9 +287,9 @@ HD void mis_push_clause(const LcveArgs& a, u32 u, u32 ru, const MisCl& cl) {
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) {
             if (w[j] == u) continue;
-            const u64 g = a.word[w[j]];
-            if (mis_rank(g) != NONE && mis_rank(g) > ru && mis_dec(g) == MIS_UNDECIDED)
-                atom_or64(&a.word[w[j]], mis_dec_bits(MIS_OUT));
+            const u32 g = a.word[w[j]];
+            if (mis_rank(g) != MIS_NO_RANK && mis_rank(g) > ru && mis_dec(g) == MIS_UNDECIDED)
+                atom_or(&a.word[w[j]], mis_dec_bits(MIS_OUT));
         }
     }
 }
@@ -311,7 +313,7 @@ HD void mis_push_vertex(const LcveArgs& a, u32 u) {
 HD void k_mis_push(const LcveArgs& a, const u32* in, u32 idx) { mis_push_vertex(a, in[idx]); }
 HD void k_mis_pull(const LcveArgs& a, const u32* in, const MisFront& und, const MisFront& ins, u32 idx) {
     const u32 v = in[idx];
-    const u64 wv = a.word[v];
+    const u32 wv = a.word[v];
     if (mis_dec(wv) != MIS_UNDECIDED) return;
     const bool big = mis_is_big(a.c, v);
     if (mis_pull_one(a, v, wv)) {
@@ -476,13 +478,13 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
         const u32* pu_b = w.u_big[r & 1];
         for (u32 idx = tid >> 5; idx < ub; idx += nwarps) {
             const u32 v = vload(&pu_b[idx]);
-            const u64 wv = vload64(&a.word[v]);
+            const u32 wv = vload(&a.word[v]);
             if (mis_dec(wv) != MIS_UNDECIDED) continue;  // warp-uniform
             const u32 rv = mis_rank(wv);
             const u32 p = V2L(v), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
             const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
             u32 stop = NONE;
-            for (u32 b0 = mis_resume(wv); b0 < n && stop == NONE; b0 += 32) {
+            for (u32 b0 = vload(&a.resume[v]); b0 < n && stop == NONE; b0 += 32) {
                 const u32 t = b0 + lane;
                 const bool blk = t < n && mis_blocked_in(a, v, rv, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])));
                 const u32 m = __ballot_sync(0xffffffffu, blk);
@@ -490,10 +492,10 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
             }
             if (lane == 0) {
                 if (stop != NONE) {
-                    a.word[v] = mis_with_resume(rv, stop);
+                    a.resume[v] = stop;
                     mis_queue_push(qu, fu, true, v);
                 } else {
-                    atomicOr((unsigned long long*)&a.word[v], (unsigned long long)mis_dec_bits(MIS_IN));
+                    atomicOr(&a.word[v], mis_dec_bits(MIS_IN));
                     mis_queue_push(qi, fi, true, v);
                 }
             }
@@ -509,7 +511,7 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
                 bool in = false, und = false;
                 if (idx < us) {
                     v = vload(&pu_s[idx]);
-                    const u64 wv = vload64(&a.word[v]);
+                    const u32 wv = vload(&a.word[v]);
                     if (mis_dec(wv) == MIS_UNDECIDED) {
                         in = mis_pull_one(a, v, wv);
                         und = !in;
@@ -530,13 +532,13 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
                 bool in = false, und = false;
                 if (idx < us) {
                     v = vload(&pu_s[idx]);
-                    const u64 wv = vload64(&a.word[v]);
+                    const u32 wv = vload(&a.word[v]);
                     if (mis_dec(wv) == MIS_UNDECIDED) {  // the same word for the whole group
                         const u32 rv = mis_rank(wv);
                         const u32 p = V2L(v), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
                         const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
                         u32 stop = NONE;
-                        for (u32 b0 = mis_resume(wv); b0 < n; b0 += lu) {
+                        for (u32 b0 = vload(&a.resume[v]); b0 < n; b0 += lu) {
                             const u32 t = b0 + sub;
                             const bool blk =
                                 t < n && mis_blocked_in(a, v, rv, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + t])));
@@ -548,10 +550,10 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
                         }
                         if (sub == 0) {
                             if (stop != NONE) {
-                                a.word[v] = mis_with_resume(rv, stop);
+                                a.resume[v] = stop;
                                 und = true;
                             } else {
-                                atom_or64(&a.word[v], mis_dec_bits(MIS_IN));
+                                atom_or(&a.word[v], mis_dec_bits(MIS_IN));
                                 in = true;
                             }
                         }
@@ -574,15 +576,15 @@ HD void k_bound_init(const LcveArgs& a, u32 f) { a.bound[2 * f + 1] = a.bound[2 
 // B = min(B0, first member whose lists reach the temperatures).
 HD void k_mis_bound(const LcveArgs& a, u32 v) {
     if (v == 0) return;
-    const u64 w = a.word[v];
-    if (mis_rank(w) != NONE && mis_dec(w) == MIS_IN && lcve_big(a, v)) atom_min(&a.bound[2 * fid_of(a.c, v) + 1], a.rank[v]);
+    const u32 w = a.word[v];
+    if (mis_rank(w) != MIS_NO_RANK && mis_dec(w) == MIS_IN && lcve_big(a, v)) atom_min(&a.bound[2 * fid_of(a.c, v) + 1], a.rank[v]);
 }
 
 // Election flags over rank positions below B (compacted by the caller in rank order).
 HD void k_elect_flag(const LcveArgs& a, u32* flags, u32 p) {
     const u32 v = a.order[p];
-    const u64 w = a.word[v];
-    flags[p] = (p < a.bound[2 * fid_of(a.c, v) + 1] && mis_rank(w) != NONE && mis_dec(w) == MIS_IN) ? 1u : 0u;
+    const u32 w = a.word[v];
+    flags[p] = (p < a.bound[2 * fid_of(a.c, v) + 1] && mis_rank(w) != MIS_NO_RANK && mis_dec(w) == MIS_IN) ? 1u : 0u;
 }
 
 HD void k_elect_write(const LcveArgs& a, const u32* flags, const u32* scan, u32 p) {

@@ -338,7 +338,7 @@ struct pf_sigma_ctx {
     // stage scratch
     DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
     DBuf<u32> mis_big_a, mis_big_b;
-    DBuf<u64> mis_word;
+    DBuf<u32> mis_word, mis_resume;
     DBuf<u32> mis_in[4];  // new-in lists of the election rounds (small x2, large x2)
     DBuf<Q4> mis_rec;  // the election's 16-byte clause records
     DBuf<u32> mis_gbits;  // the election's graph membership bitmap
@@ -919,6 +919,7 @@ struct pf_sigma_ctx {
         a.order = order.p;
         a.rank = rank.p;
         a.word = mis_word.p;
+        a.resume = mis_resume.p;
         mis_rec.reserve(rt, (size_t)ncls + 1);
         a.crec = mis_rec.p;
         mis_gbits.reserve(rt, (size_t)nvars / 32 + 1);
@@ -2176,6 +2177,7 @@ static pf_status upload_common(pf_sigma_ctx* ctx, uint32_t num_vars, const uint3
         c.flags.reserve(rt, num_vars + 1);
         c.flags_scan.reserve(rt, num_vars + 1);
         c.mis_word.reserve(rt, num_vars + 1);
+        c.mis_resume.reserve(rt, num_vars + 1);
         c.radix_hist.reserve(rt, radix_hist_elems(num_vars + 1));
         c.radix_hscan.reserve(rt, radix_hist_elems(num_vars + 1));
         c.scan_tmp32.reserve(rt, scan_tmp_elems(std::max<size_t>(radix_hist_elems(num_vars + 1), cap_cls)) + 4);
@@ -2765,6 +2767,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     for (auto* b : b64) b->free();
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
     c.mis_word.free();
+    c.mis_resume.free();
     for (auto& b : c.mis_in) b.free();
     c.mis_rec.free();
     c.mis_gbits.free();
