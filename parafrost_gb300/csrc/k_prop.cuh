@@ -290,16 +290,23 @@ HD bool prop_use_sweep(u32 pending, u32 scale, u32 ncls) { return scale && (u64)
 #if SIGMA_CUDA
 // prop_clause (Always) or prop_sweep_clause (not Always) for up to 32 clauses by one
 // warp: lane i loads the header of clause r (has: lane i holds one); the live
-// clauses' literals are then read and valued by consecutive lanes (32 literals of
-// the warp's clauses per step, all loads of a step in flight together), and lane i
+// clauses' literals are then read and valued by consecutive lanes, 32 literals of the
+// warp's clauses per step, and each literal's value is read once. Every literal that
+// is not false moves down to its place among its clause's kept literals (it is
+// written only when its place changes, so a clause without false literals is not
+// written), its signature bit goes to the clause's word in shared memory, and lane i
 // learns from the step's ballots whether its clause has a true literal and how many
-// false ones. A clause with a true literal is deleted; otherwise its false literals
-// go (the clause is rewritten when it has some, or always for Always) as the
-// per-thread versions do, whose results these are.
+// false ones. A clause with a true literal is deleted (its literal contents do not
+// matter then); otherwise, when it had false literals (or always, for Always), its
+// header takes the kept size and signature, as the per-thread versions leave it.
+// sm: 3 words per thread of the block (signature, unit, first variable of a clause).
 template <bool Always>
-DEV void prop_warp_clauses(const PropArgs& a, u32 r, bool has) {
+DEV void prop_warp_clauses(const PropArgs& a, u32* sm, u32 r, bool has) {
     const Ctx& c = a.c;
-    const u32 lane = threadIdx.x & 31u;
+    const u32 lane = threadIdx.x & 31u, wb = threadIdx.x & ~31u;
+    u32* s_sig = sm;
+    u32* s_unit = sm + blockDim.x;
+    u32* s_v0 = sm + 2 * blockDim.x;
     Hdr h;
     h.start = h.size = h.sig = h.flags = 0;
     if (has) h = ldw_hdr<true>(&c.hdr[r]);
@@ -313,8 +320,10 @@ DEV void prop_warp_clauses(const PropArgs& a, u32 r, bool has) {
     }
     const u32 excl = incl - sz;
     const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+    s_sig[wb + lane] = 0;
+    __syncwarp();
     bool sat = false;
-    u32 nfalse = 0;
+    u32 nfalse = 0, kept = 0;
     for (u32 base = 0; base < total; base += 32) {
         const u32 j = base + lane;
         u32 k = 0;  // the lane whose clause holds literal j: the first with incl > j
@@ -323,17 +332,38 @@ DEV void prop_warp_clauses(const PropArgs& a, u32 r, bool has) {
             const u32 v = __shfl_sync(0xffffffffu, incl, k + step - 1);
             if (v <= j) k += step;
         }
-        const u32 st = __shfl_sync(0xffffffffu, h.start, k & 31u), ex = __shfl_sync(0xffffffffu, excl, k & 31u);
-        const int val = j < total ? lit_value(c, ldw<true>(&c.lits[st + (j - ex)])) : VAL_UNDEF;
-        const u32 bt = __ballot_sync(0xffffffffu, val == 1), bf = __ballot_sync(0xffffffffu, val == 0);
+        k &= 31u;
+        const u32 st = __shfl_sync(0xffffffffu, h.start, k), ex = __shfl_sync(0xffffffffu, excl, k);
+        const u32 kc = __shfl_sync(0xffffffffu, kept, k);  // the clause's literals kept in earlier steps
+        const bool in = j < total;
+        const u32 lit = in ? ldw<true>(&c.lits[st + (j - ex)]) : 0u;
+        const int val = in ? lit_value(c, lit) : VAL_UNDEF;
+        const bool keep = in && val != 0;
+        const u32 bt = __ballot_sync(0xffffffffu, in && val == 1), bf = __ballot_sync(0xffffffffu, in && val == 0);
+        const u32 bk = __ballot_sync(0xffffffffu, keep);
+        if (in) {
+            const u32 pos = j - ex;  // place in the clause
+            if (pos == 0) s_v0[wb + k] = ABS(lit);
+            if (keep) {
+                // the clause's lanes of this step start at lane max(ex - base, 0)
+                const u32 lo = ex > base ? ex - base : 0u;
+                const u32 below = bk & ((1u << lane) - 1u) & ~((1u << lo) - 1u);
+                const u32 p = kc + (u32)__popc(below);
+                if (p != pos) c.lits[st + p] = lit;
+                if (p == 0) s_unit[wb + k] = lit;
+                atomicOr(&s_sig[wb + k], MAPHASH(lit));
+            }
+        }
         // this lane's literals in the step: [excl - base, incl - base) clipped to the warp
         const int lo = max((int)excl - (int)base, 0), hi = min((int)incl - (int)base, 32);
         if (lo < hi) {
             const u32 m = (hi - lo == 32 ? 0xffffffffu : ((1u << (hi - lo)) - 1u)) << lo;
             sat |= (bt & m) != 0;
             nfalse += (u32)__popc(bf & m);
+            kept += (u32)__popc(bk & m);
         }
     }
+    __syncwarp();
     if (!live) return;
     if (sat) {
         c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
@@ -341,28 +371,20 @@ DEV void prop_warp_clauses(const PropArgs& a, u32 r, bool has) {
         return;
     }
     if (!Always && !nfalse) return;
-    u32* l = c.lits + h.start;
-    const u32 v0 = ABS(ldw<true>(&l[0]));  // names the formula if the clause empties
-    u32 n = 0, sig = 0;
-    for (u32 i = 0; i < h.size; i++) {
-        const u32 lit = ldw<true>(&l[i]);
-        if (lit_value(c, lit) == 0) continue;
-        l[n++] = lit;
-        sig |= MAPHASH(lit);
-    }
+    const u32 n = kept;
     h.size = n;
-    h.sig = sig;
+    h.sig = s_sig[wb + lane];
     c.hdr[r] = h;
     touch(c, r);
     if (n == 0) {
-        set_unsat(c, v0);
+        set_unsat(c, s_v0[wb + lane]);  // names the formula the clause emptied in
         if (c.var_fid) {
             c.hdr[r].flags = (h.flags & ~3u) | ST_DELETED;
             touch(c, r);
         }
         return;
     }
-    if (n == 1) claim_unit(c, l[0]);
+    if (n == 1) claim_unit(c, s_unit[wb + lane]);
 }
 
 // Every wave of one propagation in one cooperative launch: wave A over the trail
@@ -384,7 +406,8 @@ struct PropWaves {
     u32 cap_parts;
 };
 
-__global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
+__global__ void __launch_bounds__(256, 4) prop_waves_k(PropArgs a, PropWaves w) {
+    __shared__ u32 sm[3 * 256];
     const u32 tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     u32 head = a.head;
     for (u32 wave = 0;; wave++) {
@@ -418,7 +441,7 @@ __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
         if (sweep) {
             for (u32 g = warp; g < (a.c.ncls + 31u) / 32u; g += nwarps) {
                 const u32 r = g * 32u + (tid & 31u);
-                prop_warp_clauses<false>(b, r, r < a.c.ncls);
+                prop_warp_clauses<false>(b, sm, r, r < a.c.ncls);
             }
             for (u32 i = tid; i < tail - head; i += nth) k_prop_sweep_lists(b, i);
             if (!grid_barrier(w.bar, a.c.err, a.c.ntrail, w.tail)) return;
@@ -452,7 +475,7 @@ __global__ void __launch_bounds__(256) prop_waves_k(PropArgs a, PropWaves w) {
         for (u32 g = warp; g < (nw + 31u) / 32u; g += nwarps) {
             const u32 k = g * 32u + (tid & 31u);
             const u32 r = k < nw ? __ldcg(&b.work[k]) : NONE;  // NONE: a free slot of a closed run
-            prop_warp_clauses<true>(b, r, r != NONE);
+            prop_warp_clauses<true>(b, sm, r, r != NONE);
         }
         for (u32 i = tid; i < tail - head; i += nth) k_prop_sweep_lists(b, i);
         if (!grid_barrier(w.bar, a.c.err, a.c.ntrail, w.tail)) return;
