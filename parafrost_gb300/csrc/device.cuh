@@ -352,6 +352,67 @@ HD int popc32(u32 x) {
 struct __align__(16) Q4 {
     u32 x, y, z, w;
 };
+// L2 eviction priorities for loads and stores (PTX createpolicy + .L2::cache_hint):
+// streams read once (clause records, occurrence lists, staged pairs) go first, so
+// the small arrays read again and again (independent-set words) and lines still
+// being filled by scattered stores stay in L2. In the emulation build they are
+// plain accesses.
+#if SIGMA_CUDA
+DEV u64 l2_policy_first() {
+    u64 p = 0;
+#if defined(__CUDA_ARCH__)
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+#endif
+    return p;
+}
+DEV u64 l2_policy_last() {
+    u64 p = 0;
+#if defined(__CUDA_ARCH__)
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+#endif
+    return p;
+}
+#endif
+// read-only load (no thread writes it during the launch) with a policy
+HD u32 ldro_hint(const u32* p, u64 pol) {
+#if defined(__CUDA_ARCH__)
+    u32 v;
+    asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+#else
+    (void)pol;
+    return *p;
+#endif
+}
+// load of a word other blocks write during the launch (at L2, past L1) with a policy
+HD u32 ldcg_hint(const u32* p, u64 pol) {
+#if defined(__CUDA_ARCH__)
+    u32 v;
+    asm volatile("ld.global.cg.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol) : "memory");
+    return v;
+#else
+    (void)pol;
+    return *(const volatile u32*)p;
+#endif
+}
+HD u64 ldcg_hint64(const u64* p, u64 pol) {
+#if defined(__CUDA_ARCH__)
+    u64 v;
+    asm volatile("ld.global.cg.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol) : "memory");
+    return v;
+#else
+    (void)pol;
+    return *(const volatile u64*)p;
+#endif
+}
+HD void st_hint(u32* p, u32 v, u64 pol) {
+#if defined(__CUDA_ARCH__)
+    asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+#else
+    (void)pol;
+    *p = v;
+#endif
+}
 HD Q4 ldro4(const Q4* p) {
 #if defined(__CUDA_ARCH__)
     const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
@@ -362,6 +423,18 @@ HD Q4 ldro4(const Q4* p) {
     q.w = v.w;
     return q;
 #else
+    return *p;
+#endif
+}
+HD Q4 ldro4_hint(const Q4* p, u64 pol) {
+#if defined(__CUDA_ARCH__)
+    Q4 q;
+    asm("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(q.x), "=r"(q.y), "=r"(q.z), "=r"(q.w)
+        : "l"(p), "l"(pol));
+    return q;
+#else
+    (void)pol;
     return *p;
 #endif
 }

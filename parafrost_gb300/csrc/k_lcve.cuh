@@ -46,6 +46,7 @@ struct LcveArgs {
     const u32* f_active;  // batches: formulas taking part in this election (null: all)
     u32* f_npvs;          // batches: elected variables per formula
     u32* pvs;             // elected variables in rank order
+    u64 pf = 0, pl = 0;   // L2 policies in the rounds kernel: streams go first, words last
 };
 
 // write_scores (histogram.h:32-41): eligible[v-1] = v, scores[v] = ps*ns (32-bit wrap).
@@ -136,7 +137,7 @@ struct MisCl {
 };
 HD MisCl mis_cl(const LcveArgs& a, u32 r) {
     MisCl cl;
-    cl.q = ldro4(&a.crec[r]);
+    cl.q = ldro4_hint(&a.crec[r], a.pf);
     cl.r = r;
     return cl;
 }
@@ -241,7 +242,7 @@ HD bool mis_blocked_in(const LcveArgs& a, u32 v, u32 rv, const MisCl& cl) {
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) {
             if (w[j] == v) continue;
-            const u32 g = vload(&a.word[w[j]]);
+            const u32 g = ldcg_hint(&a.word[w[j]], a.pl);
             b |= mis_rank(g) < rv && mis_dec(g) != MIS_OUT;
         }
         if (b) return true;
@@ -258,10 +259,10 @@ HD bool mis_pull_one(const LcveArgs& a, u32 v, u32 wv) {
     const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
     u32 t = vload(&a.resume[v]);
     if (t < n) {
-        MisCl cl = mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + t]));
+        MisCl cl = mis_cl(a, ldro_hint(&a.c.ot_refs[t < np ? op + t : on + t], a.pf));
         for (; t < n; t++) {
             MisCl nx = cl;
-            if (t + 1 < n) nx = mis_cl(a, ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1]));
+            if (t + 1 < n) nx = mis_cl(a, ldro_hint(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1], a.pf));
             if (mis_blocked_in(a, v, rv, cl)) {
                 a.resume[v] = t;
                 return false;
@@ -287,7 +288,7 @@ HD void mis_push_clause(const LcveArgs& a, u32 u, u32 ru, const MisCl& cl) {
 #pragma unroll
         for (u32 j = 0; j < MIS_CHUNK; j++) {
             if (w[j] == u) continue;
-            const u32 g = a.word[w[j]];
+            const u32 g = ldcg_hint(&a.word[w[j]], a.pl);
             if (mis_rank(g) != MIS_NO_RANK && mis_rank(g) > ru && mis_dec(g) == MIS_UNDECIDED)
                 atom_or(&a.word[w[j]], mis_dec_bits(MIS_OUT));
         }
@@ -299,10 +300,10 @@ HD void mis_push_vertex(const LcveArgs& a, u32 u) {
     const u32 p = V2L(u), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
     const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
     if (!n) return;
-    MisCl cl = mis_cl(a, ldro(&a.c.ot_refs[op]));
+    MisCl cl = mis_cl(a, ldro_hint(&a.c.ot_refs[op], a.pf));
     for (u32 t = 0; t < n; t++) {
         MisCl nx = cl;
-        if (t + 1 < n) nx = mis_cl(a, ldro(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1]));
+        if (t + 1 < n) nx = mis_cl(a, ldro_hint(&a.c.ot_refs[t + 1 < np ? op + t + 1 : on + t + 1], a.pf));
         mis_push_clause(a, u, ru, cl);
         cl = nx;
     }
@@ -409,7 +410,10 @@ DEV void mis_queue_flush(MisBlockQueue& q, const MisFront& f) {
     if (threadIdx.x == 0) q.ns = q.nb = 0;
 }
 
-__global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
+__global__ void __launch_bounds__(256, 6) mis_rounds_k(LcveArgs a0, MisRounds w) {
+    LcveArgs a = a0;
+    a.pf = l2_policy_first();
+    a.pl = l2_policy_last();
     __shared__ MisBlockQueue qu, qi;
     const u32 tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const u32 lane = threadIdx.x & 31u, nwarps = nth >> 5;
@@ -445,7 +449,7 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
             const u32 p = V2L(u), np = a.c.ot_size[p], nn = a.c.ot_size[p + 1];
             const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1];
             for (u32 t = lane; t < np + nn; t += 32)
-                mis_push_clause(a, u, ru, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])));
+                mis_push_clause(a, u, ru, mis_cl(a, ldro_hint(&a.c.ot_refs[t < np ? op + t : on + (t - np)], a.pf)));
             __syncwarp();
         }
         const u32* pin_s = w.in_small[r & 1];
@@ -461,7 +465,7 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
                 const u32 p = V2L(u), np = a.c.ot_size[p], n = np + a.c.ot_size[p + 1];
                 const u32 op = a.c.ot_off[p], on = a.c.ot_off[p + 1] - np;
                 for (u32 t = sub; t < n; t += li)
-                    mis_push_clause(a, u, ru, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + t])));
+                    mis_push_clause(a, u, ru, mis_cl(a, ldro_hint(&a.c.ot_refs[t < np ? op + t : on + t], a.pf)));
             }
         }
         if (!grid_barrier(w.bar, a.c.err)) return;
@@ -486,7 +490,7 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
             u32 stop = NONE;
             for (u32 b0 = vload(&a.resume[v]); b0 < n && stop == NONE; b0 += 32) {
                 const u32 t = b0 + lane;
-                const bool blk = t < n && mis_blocked_in(a, v, rv, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + (t - np)])));
+                const bool blk = t < n && mis_blocked_in(a, v, rv, mis_cl(a, ldro_hint(&a.c.ot_refs[t < np ? op + t : on + (t - np)], a.pf)));
                 const u32 m = __ballot_sync(0xffffffffu, blk);
                 if (m) stop = b0 + (u32)(__ffs(m) - 1);
             }
@@ -541,7 +545,7 @@ __global__ void __launch_bounds__(256) mis_rounds_k(LcveArgs a, MisRounds w) {
                         for (u32 b0 = vload(&a.resume[v]); b0 < n; b0 += lu) {
                             const u32 t = b0 + sub;
                             const bool blk =
-                                t < n && mis_blocked_in(a, v, rv, mis_cl(a, ldro(&a.c.ot_refs[t < np ? op + t : on + t])));
+                                t < n && mis_blocked_in(a, v, rv, mis_cl(a, ldro_hint(&a.c.ot_refs[t < np ? op + t : on + t], a.pf)));
                             const u32 m = (__ballot_sync(gmask, blk) & gmask) >> gbase;
                             if (m) {
                                 stop = b0 + (u32)(__ffs(m) - 1);

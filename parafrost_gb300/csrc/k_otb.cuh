@@ -209,12 +209,15 @@ __global__ void __launch_bounds__(OTB_LIST_THREADS) ot_bucket_lists_k(OtbArgs a)
     for (u32 i = tid; i < nl; i += blockDim.x) otb_cnt[i] = 0;
     if (tid == 0) carry = 0;
     __syncthreads();
-    // four occurrences per thread per step, their loads issued before the atomics
+    // four occurrences per thread per step, their loads issued before the atomics; the
+    // staged pairs are read twice and then dead (evicted first), the lists' lines are
+    // filled by scattered stores and kept while they fill
+    const u64 pf = l2_policy_first(), pl = l2_policy_last();
     const u32 step = 4u * blockDim.x;
     for (u32 k0 = p0 + tid; k0 < p1; k0 += step) {
         u64 x[4];
 #pragma unroll
-        for (u32 j = 0; j < 4; j++) x[j] = k0 + j * blockDim.x < p1 ? __ldcg(&a.tpair[k0 + j * blockDim.x]) : 0ull;
+        for (u32 j = 0; j < 4; j++) x[j] = k0 + j * blockDim.x < p1 ? ldcg_hint64(&a.tpair[k0 + j * blockDim.x], pf) : 0ull;
 #pragma unroll
         for (u32 j = 0; j < 4; j++)
             if (k0 + j * blockDim.x < p1) atomicAdd(&otb_cnt[(u32)x[j] - l0], 1u);
@@ -247,10 +250,11 @@ __global__ void __launch_bounds__(OTB_LIST_THREADS) ot_bucket_lists_k(OtbArgs a)
     for (u32 k0 = p0 + tid; k0 < p1; k0 += step) {
         u64 x[4];
 #pragma unroll
-        for (u32 j = 0; j < 4; j++) x[j] = k0 + j * blockDim.x < p1 ? __ldcs(&a.tpair[k0 + j * blockDim.x]) : 0ull;
+        for (u32 j = 0; j < 4; j++) x[j] = k0 + j * blockDim.x < p1 ? ldcg_hint64(&a.tpair[k0 + j * blockDim.x], pf) : 0ull;
 #pragma unroll
         for (u32 j = 0; j < 4; j++)
-            if (k0 + j * blockDim.x < p1) a.c.ot_refs[p0 + atomicAdd(&otb_cnt[(u32)x[j] - l0], 1u)] = (u32)(x[j] >> 32);
+            if (k0 + j * blockDim.x < p1)
+                st_hint(&a.c.ot_refs[p0 + atomicAdd(&otb_cnt[(u32)x[j] - l0], 1u)], (u32)(x[j] >> 32), pl);
     }
 }
 
