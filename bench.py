@@ -256,7 +256,7 @@ def profiled_utilisation(kernel: str, workload: str):
     if not kv or "sm_pct" not in kv:
         return None
     return {"sm_throughput_pct": float(kv["sm_pct"]), "dram_throughput_pct": float(kv["dram_pct"]),
-            "launch": kv.get("measured_launch"), "source": "profiles/dram_traffic.txt (ncu --set full)"}
+            "launch": kv.get("measured_launch"), "source": "profiles/dram_traffic.txt (ncu captures named there)"}
 
 
 def phase_rows(stats, peak: float) -> list:
