@@ -327,6 +327,19 @@ HD u32 upper_segment(const T* start, u32 n, T key) {
     return lo;
 }
 
+#if SIGMA_CUDA
+// Work of the per-variable warp kernels: warps take elected variables from one counter
+// in work order (longest lists first), kWarpChunkFar at a time while more than
+// kWarpFarLeft variables a warp are left (millions of elected variables: fewer atomics
+// on the counter), else kWarpChunkNear at a time (measured: larger chunks slow the
+// AIG workload's 0.8M-variable phases, where a warp's share is about 80 variables).
+constexpr u32 kWarpChunkFar = 16, kWarpChunkNear = 4, kWarpFarLeft = 128;
+DEV u32 warp_chunk(u32 left) {
+    const u32 warps = (gridDim.x * blockDim.x) >> 5;
+    return (u64)left > (u64)warps * kWarpFarLeft ? kWarpChunkFar : kWarpChunkNear;
+}
+#endif
+
 // Volatile load for values that other threads of the same launch may update.
 HD u32 vload(const u32* p) { return *(const volatile u32*)p; }
 HD u64 vload64(const u64* p) { return *(const volatile u64*)p; }

@@ -67,13 +67,15 @@ HD void bce_count_warp(const BceArgs& a, u32 k) {
 // Warps take elected variables in work order (perm), a few at a time.
 __global__ void __launch_bounds__(256) bce_count_warp_k(BceArgs a, const u32* perm, u32 npos, u32* next) {
     const u32 lane = threadIdx.x & 31u;
+    u32 chunk = warp_chunk(npos);
     while (true) {
         u32 j0 = 0;
-        if (lane == 0) j0 = atomicAdd(next, 4u);
+        if (lane == 0) j0 = atomicAdd(next, chunk);
         j0 = __shfl_sync(0xffffffffu, j0, 0);
         if (j0 >= npos) break;
-        const u32 j1 = j0 + 4u < npos ? j0 + 4u : npos;
+        const u32 j1 = j0 + chunk < npos ? j0 + chunk : npos;
         for (u32 j = j0; j < j1; j++) bce_count_warp(a, perm[j]);
+        chunk = warp_chunk(npos - j1);
     }
 }
 #endif

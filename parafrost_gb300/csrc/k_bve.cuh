@@ -158,18 +158,19 @@ HD void bve_warp_one(const BveArgs& a, u32 k, u32* slot) {
 
 #if SIGMA_CUDA
 constexpr int kBveWarpThreads = 256;
-constexpr u32 kBveWarpChunk = 4;  // variables a warp takes per counter increment
 __global__ void __launch_bounds__(kBveWarpThreads, 6) bve_warp_k(BveArgs a, const u32* perm, u32* next) {
     extern __shared__ u32 smem[];
     u32* slot = smem + (threadIdx.x >> 5) * WPV_WORDS;
     const u32 lane = threadIdx.x & 31u;
+    u32 chunk = warp_chunk(a.npvs);
     while (true) {
         u32 j0 = 0;
-        if (lane == 0) j0 = atomicAdd(next, kBveWarpChunk);
+        if (lane == 0) j0 = atomicAdd(next, chunk);
         j0 = __shfl_sync(0xffffffffu, j0, 0);
         if (j0 >= a.npvs) break;
-        const u32 j1 = j0 + kBveWarpChunk < a.npvs ? j0 + kBveWarpChunk : a.npvs;
+        const u32 j1 = j0 + chunk < a.npvs ? j0 + chunk : a.npvs;
         for (u32 j = j0; j < j1; j++) bve_warp_one(a, perm[j], slot);
+        chunk = warp_chunk(a.npvs - j1);
     }
 }
 #endif
@@ -459,13 +460,15 @@ __device__ void bve_write_warp(const BveArgs& a, u32 k) {
 
 __global__ void __launch_bounds__(256, 6) bve_write_warp_k(BveArgs a, const u32* perm, u32 npos, u32* next) {
     const u32 lane = threadIdx.x & 31u;
+    u32 chunk = warp_chunk(npos);
     while (true) {
         u32 j0 = 0;
-        if (lane == 0) j0 = atomicAdd(next, 4u);
+        if (lane == 0) j0 = atomicAdd(next, chunk);
         j0 = __shfl_sync(0xffffffffu, j0, 0);
         if (j0 >= npos) break;
-        const u32 j1 = j0 + 4u < npos ? j0 + 4u : npos;
+        const u32 j1 = j0 + chunk < npos ? j0 + chunk : npos;
         for (u32 j = j0; j < j1; j++) bve_write_warp(a, perm[j]);
+        chunk = warp_chunk(npos - j1);
     }
 }
 #endif

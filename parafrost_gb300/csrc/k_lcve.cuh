@@ -120,6 +120,55 @@ HD void k_mis_init(const LcveArgs& a, const MisFront& und, u32 v) {
     mis_append(und, a.c, v, in_graph);
 }
 
+#if SIGMA_CUDA
+// k_mis_init over variables 0..n-1 with block-wide appends: a block takes 256
+// consecutive variables a step, ranks its small and big vertices by warp ballots and
+// reserves both lists' places with one atomic each (the lists' two counters would
+// otherwise take one atomic per warp step over 20M variables); lane 0 of a warp
+// writes its 32 variables' membership word.
+__global__ void __launch_bounds__(256) mis_init_k(LcveArgs a, MisFront und, u32 n) {
+    __shared__ u32 ws[8], wb[8], base_s, base_b;
+    const u32 lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (u32 v0 = blockIdx.x * 256u; v0 < n; v0 += gridDim.x * 256u) {
+        const u32 v = v0 + threadIdx.x;
+        bool in_graph = false, big = false;
+        if (v < n) {
+            const u32 f = v ? fid_of(a.c, v) : 0u;
+            in_graph = v && (!a.f_active || a.f_active[f]) && lcve_valid(a.c, v) && lcve_freezable(a, v) &&
+                       a.rank[v] < a.bound[2 * f];
+            a.word[v] = in_graph ? a.rank[v] : MIS_NO_RANK;
+            a.resume[v] = 0;
+            big = in_graph && mis_is_big(a.c, v);
+        }
+        const u32 gm = __ballot_sync(kFull, in_graph);
+        if (lane == 0 && v < n) a.gbits[v >> 5] = gm;
+        const u32 ms = __ballot_sync(kFull, in_graph && !big), mb = __ballot_sync(kFull, big);
+        if (lane == 0) {
+            ws[warp] = (u32)__popc(ms);
+            wb[warp] = (u32)__popc(mb);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u32 ts = 0, tb = 0;
+            for (u32 k = 0; k < 8; k++) {
+                const u32 xs = ws[k], xb = wb[k];
+                ws[k] = ts;
+                wb[k] = tb;
+                ts += xs;
+                tb += xb;
+            }
+            base_s = ts ? atomicAdd(und.nsmall, ts) : 0u;
+            base_b = tb ? atomicAdd(und.nbig, tb) : 0u;
+        }
+        __syncthreads();
+        const u32 below = (1u << lane) - 1u;
+        if (in_graph && !big) und.small[base_s + ws[warp] + (u32)__popc(ms & below)] = v;
+        if (big) und.big[base_b + wb[warp] + (u32)__popc(mb & below)] = v;
+        __syncthreads();
+    }
+}
+#endif
+
 // The clause walks read literals four at a time, so the loads (and the pushes'
 // atomics) of a chunk are in flight together. Clauses and lists are not written
 // while the independent set is decided.

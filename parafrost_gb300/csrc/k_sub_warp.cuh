@@ -85,18 +85,18 @@ HD void sub_warp_pv(const SubArgs& a, u32 k) {
 }
 
 #if SIGMA_CUDA
-constexpr u32 kSubWarpChunk = 4;
-
 // Warps take elected variables in work order (perm), a few at a time.
 __global__ void __launch_bounds__(256, 8) sub_warp_k(SubArgs a, const u32* perm, u32 n, u32* next) {
     const u32 lane = threadIdx.x & 31u;
+    u32 chunk = warp_chunk(n);
     while (true) {
         u32 j0 = 0;
-        if (lane == 0) j0 = atomicAdd(next, kSubWarpChunk);
+        if (lane == 0) j0 = atomicAdd(next, chunk);
         j0 = __shfl_sync(0xffffffffu, j0, 0);
         if (j0 >= n) break;
-        const u32 j1 = j0 + kSubWarpChunk < n ? j0 + kSubWarpChunk : n;
+        const u32 j1 = j0 + chunk < n ? j0 + chunk : n;
         for (u32 j = j0; j < j1; j++) sub_warp_pv(a, perm[j]);
+        chunk = warp_chunk(n - j1);
     }
 }
 #endif

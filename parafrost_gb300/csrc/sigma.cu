@@ -952,7 +952,14 @@ struct pf_sigma_ctx {
         for (auto& b : mis_in) b.reserve(rt, nvars + 1);
         u32* ctr = counters.p + 12;  // [12..23] three sets of list lengths, [24..25] barrier, [26] rounds
         rt.zero(ctr, 15 * 4);
+#if SIGMA_CUDA
+        rt.launches++;
+        mis_init_k<<<rt.grid(nvars + 1), 256, 0, rt.stream>>>(
+            a, MisFront{flags.p, ctr, mis_big_a.p, ctr + 1}, nvars + 1);
+        ck(cudaGetLastError(), "launch");
+#else
         rt.each(FMisInit{a, MisFront{flags.p, ctr, mis_big_a.p, ctr + 1}}, nvars + 1);
+#endif
 #if SIGMA_CUDA
         if (ncls) {
             rt.launches++;
