@@ -28,7 +28,8 @@ namespace sigma {
 #if SIGMA_CUDA
 
 constexpr u32 OTB_TILE = 4096;      // clauses per block tile in pass 0
-constexpr u32 OTB_FILL_CAP = 8192;   // occurrences of a pass-1 tile ordered in shared memory
+constexpr u32 OTB_FILL_CAP = 6144;   // occurrences of a pass-1 tile ordered in shared memory
+                                     // (48 KB: three 512-thread blocks per SM)
 constexpr u32 OTB_MAX_BUCKETS = 4096;
 constexpr u32 OTB_MAX_SHIFT = 15;   // 32,768 slots: 128 KiB of shared counters in pass 2
 constexpr u32 OTB_LIST_THREADS = 1024;  // one block a bucket, 32 warps to keep its loads in flight

@@ -723,7 +723,11 @@ struct pf_sigma_ctx {
         const u32 ntiles = (ncls + fill_tile - 1) / fill_tile;
         if (ntiles) {
             rt.launches++;
-            ot_bucket_fill_k<<<std::min((u32)rt.sms * 2u, ntiles), OTB_FILL_THREADS, fill_smem, rt.stream>>>(a);
+            int per_sm = 0;
+            ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ot_bucket_fill_k, OTB_FILL_THREADS, fill_smem),
+               "occupancy");
+            const u32 fill_grid = std::min((u32)rt.sms * (u32)std::max(per_sm, 1), ntiles);
+            ot_bucket_fill_k<<<fill_grid, OTB_FILL_THREADS, fill_smem, rt.stream>>>(a);
             ck(cudaGetLastError(), "launch");
         }
         rt.launches++;
