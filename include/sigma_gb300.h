@@ -69,7 +69,7 @@ typedef struct {
                               * per-literal counters outgrow the L2 cache), 1 always literal
                               * buckets, -1 always per-occurrence atomics */
     int32_t sweep_div;       /* propagation sweeps the whole store when the pending literals'
-                              * lists exceed 1/sweep_div of it: 0 = 16, -1 never sweeps */
+                              * lists exceed 1/sweep_div of it: 0 = 64, -1 never sweeps */
     int32_t pv_blocks;       /* blocks per SM of the per-variable warp kernels: 0 = 8 */
     int32_t reserved[2];
 } pf_options;

@@ -775,7 +775,7 @@ struct pf_sigma_ctx {
     // sweep divisor, 0 when sweeps are off (prop_use_sweep).
     u32 sweep_scale() const {
         if (opt.sweep_div < 0) return 0;
-        const u64 div = opt.sweep_div ? (u64)opt.sweep_div : 16ull;
+        const u64 div = opt.sweep_div ? (u64)opt.sweep_div : 64ull;
         return (u32)std::min<u64>(std::max<u64>(div * nlits_used / std::max<u32>(D, 1), 1), 0xFFFFFFFFull);
     }
     // Blocks of the per-variable warp kernels.

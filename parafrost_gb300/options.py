@@ -54,7 +54,7 @@ class Options:
     loop_limit: int = 0  # device-side loop rounds before PF_ETIMEOUT (0: variables + 2)
     proof: int = 0  # 1: record the round's DRAT proof (reference option "proof")
     ot_buckets: int = 0  # occurrence-table build: 0 by size, 1 literal buckets, -1 atomics
-    sweep_div: int = 0  # propagation sweeps when pending lists exceed 1/sweep_div of the store (0: 16, -1: never)
+    sweep_div: int = 0  # propagation sweeps when pending lists exceed 1/sweep_div of the store (0: 64, -1: never)
     pv_blocks: int = 0  # blocks per SM of the per-variable warp kernels (0: 8)
 
     def derived(self) -> "Options":

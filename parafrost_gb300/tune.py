@@ -28,7 +28,7 @@ from .sigma import Simplifier
 
 CANDIDATES = {
     "ot_buckets": (-1, 1),
-    "sweep_div": (4, 16, 64, -1),
+    "sweep_div": (16, 64, 256, -1),
     "pv_blocks": (4, 8, 16),
 }
 
