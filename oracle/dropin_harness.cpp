@@ -1,8 +1,8 @@
 /*
  * Drop-in harness: the UNMODIFIED reference ParaFROST solver (compiled from its own
  * sources by oracle/ref.mk) with its preprocessing sigmify round handed to this
- * repository's C ABI through the C++ mirror include/sigma_gb300.hpp, exactly where
- * INTEGRATION.md puts it. Test infrastructure only.
+ * repository's C ABI through the C++ mirror include/sigma_gb300.hpp, in place of the
+ * round's phase loop inside sigmifying(). Test infrastructure only.
  *
  * sigmify_gb300() is ParaFROST::sigmifying() (src/cpu/simplify.cpp:157-232) with its
  * phase loop (lines 184-197) replaced by pfrost_gb300::Sigma: the solver's own
