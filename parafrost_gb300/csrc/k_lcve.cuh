@@ -47,6 +47,9 @@ struct LcveArgs {
     u32* f_npvs;          // batches: elected variables per formula
     u32* pvs;             // elected variables in rank order
     u64 pf = 0, pl = 0;   // L2 policies in the rounds kernel: streams go first, words last
+    u32* cmin;            // per clause: the least rank of its graph vertices (MIS_NO_RANK when
+                          // it has none or is deleted), built with the clause records
+    bool r0 = false;      // the first round's pull: walks test cmin instead of the neighbours
 };
 
 // write_scores (histogram.h:32-41): eligible[v-1] = v, scores[v] = ps*ns (32-bit wrap).
@@ -178,16 +181,27 @@ constexpr u32 MIS_CHUNK = 4;
 // literals and its size and deleted bit (built once per election by k_mis_rec), so
 // clauses of up to three literals cost one load; longer ones read the rest of
 // their literals from the store.
+// In the first round no vertex is out yet, so a clause stops a walk of v exactly when
+// one of its graph vertices ranks below v: when its least rank (cmin) is below v's.
+// The first round's walks then load one word per clause (kept in q.x) instead of the
+// record and the neighbours' words.
 struct MisCl {
     Q4 q;
     u32 r;
-    HD bool deleted() const { return (q.w >> 31) != 0; }
+    bool r0;
+    HD bool deleted() const { return !r0 && (q.w >> 31) != 0; }
     HD u32 size() const { return q.w & 0x7FFFFFFFu; }
 };
 HD MisCl mis_cl(const LcveArgs& a, u32 r) {
     MisCl cl;
-    cl.q = ldro4_hint(&a.crec[r], a.pf);
     cl.r = r;
+    cl.r0 = a.r0;
+    if (a.r0) {
+        cl.q.x = ldro_hint(&a.cmin[r], a.pf);
+        cl.q.y = cl.q.z = cl.q.w = 0;
+    } else {
+        cl.q = ldro4_hint(&a.crec[r], a.pf);
+    }
     return cl;
 }
 // Literal k of the clause; L is the clause's literal array (read only for k >= 3).
@@ -211,11 +225,14 @@ HD void k_mis_rec(const LcveArgs& a, Q4* rec, u32 i) {
     q.z = h.size > 2 ? l[2] : 0u;
     q.w = h.size | (h_deleted(h.flags) ? 0x80000000u : 0u);
     rec[i] = q;
-    u32 ng = 0;
+    u32 ng = 0, m = MIS_NO_RANK;
     for (u32 k = 0; k < h.size; k++) {
         const u32 x = ABS(l[k]);
         ng += (ldro(&a.gbits[x >> 5]) >> (x & 31u)) & 1u;
+        const u32 rk = mis_rank(a.word[x]);
+        if (rk < m) m = rk;
     }
+    a.cmin[i] = h_deleted(h.flags) ? MIS_NO_RANK : m;
     spread_sum_add64(a.ws_bytes, (u64)ng * (4ull + (h_deleted(h.flags) ? 0ull : 8ull + 4ull * h.size)));
 }
 
@@ -226,6 +243,7 @@ HD void k_mis_rec(const LcveArgs& a, Q4* rec, u32 i) {
 // literal of a graph vertex adding 4 bytes and, in a live clause, the clause's
 // 8 + 4 * len bytes.
 __global__ void __launch_bounds__(256) mis_rec_warp_k(LcveArgs a, Q4* rec) {
+    __shared__ u32 s_min[256];  // per lane of the block: the least rank of its clause
     const u32 lane = threadIdx.x & 31u;
     const u32 nw = (gridDim.x * blockDim.x) >> 5;
     const u32 ngroups = (a.c.ncls + 31u) / 32u;
@@ -234,6 +252,9 @@ __global__ void __launch_bounds__(256) mis_rec_warp_k(LcveArgs a, Q4* rec) {
         const u32 id0 = g * 32u;
         const u32 n = a.c.ncls - id0 < 32u ? a.c.ncls - id0 : 32u;
         u32 start = 0, sz = 0, weight = 0;
+        bool dead = true;
+        s_min[threadIdx.x] = MIS_NO_RANK;
+        __syncwarp();
         if (lane < n) {
             const Hdr h = hdr_ro(&a.c.hdr[id0 + lane]);
             const u32* l = a.c.lits + h.start;
@@ -246,6 +267,7 @@ __global__ void __launch_bounds__(256) mis_rec_warp_k(LcveArgs a, Q4* rec) {
             start = h.start;
             sz = h.size;
             weight = 4u + (h_deleted(h.flags) ? 0u : 8u + 4u * h.size);
+            dead = h_deleted(h.flags);
         }
         u32 incl = sz;
 #pragma unroll
@@ -267,9 +289,14 @@ __global__ void __launch_bounds__(256) mis_rec_warp_k(LcveArgs a, Q4* rec) {
             const u32 wt = __shfl_sync(0xffffffffu, weight, k & 31u);
             if (j < total) {
                 const u32 x = ABS(__ldg(&a.c.lits[st + (j - ex)]));
-                if ((ldro(&a.gbits[x >> 5]) >> (x & 31u)) & 1u) sum += wt;
+                if ((ldro(&a.gbits[x >> 5]) >> (x & 31u)) & 1u) {
+                    sum += wt;
+                    atomicMin(&s_min[(threadIdx.x & ~31u) + (k & 31u)], mis_rank(ldro(&a.word[x])));
+                }
             }
         }
+        __syncwarp();
+        if (lane < n) a.cmin[id0 + lane] = dead ? MIS_NO_RANK : s_min[threadIdx.x];
     }
     for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if (lane == 0 && sum) atomicAdd((unsigned long long*)(a.ws_bytes + (blockIdx.x & (kSpreadSlots - 1u))),
@@ -280,6 +307,7 @@ __global__ void __launch_bounds__(256) mis_rec_warp_k(LcveArgs a, Q4* rec) {
 // Whether clause cl holds a graph neighbour of v ranked below rv that is not out
 // (decisions are read through to the cache level other SMs write).
 HD bool mis_blocked_in(const LcveArgs& a, u32 v, u32 rv, const MisCl& cl) {
+    if (cl.r0) return cl.q.x < rv;
     if (cl.deleted()) return false;
     const u32 size = cl.size();
     const u32* L = mis_long_lits(a, cl);
@@ -469,6 +497,7 @@ __global__ void __launch_bounds__(256, 6) mis_rounds_k(LcveArgs a0, MisRounds w)
     if (threadIdx.x == 0) qu.ns = qu.nb = qi.ns = qi.nb = 0;
     __syncthreads();
     for (u32 r = 0;; r++) {
+        a.r0 = r == 0;
         const u32 cur = r % 3, nxt = (r + 1) % 3, old = (r + 2) % 3;
         const u32 us = vload(&w.ctr[4 * cur]), ub = vload(&w.ctr[4 * cur + 1]);
         const u32 is = vload(&w.ctr[4 * cur + 2]), ib = vload(&w.ctr[4 * cur + 3]);

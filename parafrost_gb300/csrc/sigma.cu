@@ -338,7 +338,7 @@ struct pf_sigma_ctx {
     // stage scratch
     DBuf<u32> score, order, order_k2, order_v2, rank, bound, pvs, flags, flags_scan;
     DBuf<u32> mis_big_a, mis_big_b;
-    DBuf<u32> mis_word, mis_resume;
+    DBuf<u32> mis_word, mis_resume, mis_cmin;
     DBuf<u32> mis_in[4];  // new-in lists of the election rounds (small x2, large x2)
     DBuf<Q4> mis_rec;  // the election's 16-byte clause records
     DBuf<u32> mis_gbits;  // the election's graph membership bitmap
@@ -926,6 +926,8 @@ struct pf_sigma_ctx {
         a.resume = mis_resume.p;
         mis_rec.reserve(rt, (size_t)ncls + 1);
         a.crec = mis_rec.p;
+        mis_cmin.reserve(rt, (size_t)ncls + 1);
+        a.cmin = mis_cmin.p;
         mis_gbits.reserve(rt, (size_t)nvars / 32 + 1);
         rt.zero(mis_gbits.p, ((size_t)nvars / 32 + 1) * 4);
         a.gbits = mis_gbits.p;
@@ -1014,8 +1016,10 @@ struct pf_sigma_ctx {
             if (n[2]) rt.each(FMisPush{a, ins[cur].small}, n[2]);
             if (n[3]) rt.each(FMisPush{a, ins[cur].big}, n[3]);
             rt.zero(ctr + 4 * (cur ^ 1u), 16);
-            if (n[0]) rt.each(FMisPull{a, und[cur].small, und[cur ^ 1u], ins[cur ^ 1u]}, n[0]);
-            if (n[1]) rt.each(FMisPull{a, und[cur].big, und[cur ^ 1u], ins[cur ^ 1u]}, n[1]);
+            LcveArgs ar = a;
+            ar.r0 = rounds == 1;  // the first round's walks test the clauses' least ranks
+            if (n[0]) rt.each(FMisPull{ar, und[cur].small, und[cur ^ 1u], ins[cur ^ 1u]}, n[0]);
+            if (n[1]) rt.each(FMisPull{ar, und[cur].big, und[cur ^ 1u], ins[cur ^ 1u]}, n[1]);
         }
         kclock[K_MIS].stop(rt);
 #endif
@@ -2779,6 +2783,7 @@ void pf_sigma_destroy(pf_sigma_ctx* ctx) {
     DBuf<uint8_t>* b8[] = {&c.vstate, &c.ve_type, &c.sub_run};
     c.mis_word.free();
     c.mis_resume.free();
+    c.mis_cmin.free();
     for (auto& b : c.mis_in) b.free();
     c.mis_rec.free();
     c.mis_gbits.free();
