@@ -21,6 +21,15 @@ def test_profiled_lines_for_the_hot_kernels():
     assert bench.profiled_traffic("mis_rounds", "no-such-workload") is None
 
 
+def test_profiled_line_for_the_default_workload():
+    # the default workload's election traffic, measured at full size, rides along in the
+    # benchmark line beside the algorithmic bytes it is compared with
+    t = bench.profiled_traffic("mis_rounds", "community-20m")
+    assert t and t > 1e9
+    u = bench.profiled_utilisation("mis_rounds", "community-20m")
+    assert u and 0 < u["dram_throughput_pct"] <= 100 and u["launch"] == "round_average"
+
+
 def test_result_buffers_grow_and_reuse():
     sizes = []
     buf = ResultBuffers(lambda n: sizes.append(n) or np.empty(n, dtype=np.uint8))
